@@ -1,0 +1,420 @@
+#!/usr/bin/env python
+"""Benchmark: JTransforms' transform path on GB300.
+
+Headline workload (one JSON line): FloatFFT_1D.complexForward batched at
+n = 2^10, 2^14, 2^18, 2^20, 2^24, each a 1 GiB complex64 array
+(batch = 2^27 / n), inputs i.i.d. N(0,1) re/im from a seeded generator.
+A step runs the five 1 GiB batches once.  GFLOP/s uses 5 N log2 N per
+transform.  The other workloads (256 x DoubleFFT_1D(4096) forward+inverse,
+FloatFFT_2D(2048^2).realForward, DoubleDCT_2D(1024^2).forward(true),
+DoubleFFT_3D(256^3).complexForward, DoubleDST_3D/DoubleDHT_3D(128^3).forward,
+10,000 mixed 1D transforms) are reported under "other_workloads".
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference (oracle/, no JDK
+on the box to run JTransforms itself) on all host cores for the same
+workload, on a bounded sample of each batch.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZES = [2 ** 10, 2 ** 14, 2 ** 18, 2 ** 20, 2 ** 24]
+ELEMS = 2 ** 27          # complex elements per size per rank (1 GiB complex64)
+SEED = 20110602
+METRIC = "GFLOP/s (5N log2N) & % HBM roofline; TC-split vs plain FP32 at same error"
+UNIT = "GFLOP/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def flops_c2c(n, batch):
+    return 5.0 * n * math.log2(n) * batch
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ----------------------------------------------------------------------------
+# reference arm: the oracle (CPU restatement of JTransforms) on host cores
+# ----------------------------------------------------------------------------
+def cpu_sample(budget_s: float = 3.0, threads: int = 0):
+    """Times the oracle on a bounded sample of each headline batch.  Returns
+    (GFLOP/s, threads, description)."""
+    from oracle import oracle as O
+    O.build()
+    nthreads = threads or O.max_threads()
+    rng = np.random.default_rng(SEED)
+    tot_flops, tot_time, parts = 0.0, 0.0, []
+    for n in SIZES:
+        batch = ELEMS // n
+        x1 = rng.standard_normal(2 * n).astype(np.float32)
+        t0 = time.perf_counter()
+        O.run(O.FFT, O.COMPLEX_FORWARD, [n], x1)
+        t1 = time.perf_counter() - t0
+        per_thread = max(1, int(budget_s / max(t1, 1e-6)))
+        count = int(min(batch, max(1, per_thread * nthreads)))
+        x = rng.standard_normal(2 * n * count).astype(np.float32)
+        t0 = time.perf_counter()
+        O.run_batch(O.FFT, O.COMPLEX_FORWARD, [n], x, count, 2 * n, False, nthreads)
+        dt = time.perf_counter() - t0
+        tot_flops += flops_c2c(n, count)
+        tot_time += dt
+        parts.append(f"2^{int(math.log2(n))}x{count}")
+    return tot_flops / tot_time / 1e9, nthreads, "oracle complexForward on " + ", ".join(parts) + " of the 1 GiB batches"
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    vals = []
+    kind = "port"
+    threads = 0
+    desc = ""
+    for _ in range(args.warmup):
+        cpu_sample(0.3)
+    for _ in range(args.steps):
+        v, threads, desc = cpu_sample(1.0)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded N(0,1))",
+            "config": headline_config(args),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "JTransforms is Java and no JDK exists on the box; the reference arm runs oracle/jt_oracle.cpp, "
+                    "a C++ restatement of its algorithms, with OpenMP across the batch"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def headline_config(args):
+    return {"workload": "FloatFFT_1D.complexForward batched, n=2^10,2^14,2^18,2^20,2^24, 1 GiB complex64 each "
+                        "(batch=2^27/n), inputs N(0,1)",
+            "sizes": SIZES, "elems_per_size": ELEMS, "global_batch": [ELEMS // n for n in SIZES],
+            "parallelism": f"replicas{args.gpus}",
+            "l2": "inputs 1 GiB > L2; a 256 MiB buffer is also written before each timed call",
+            "mode": "plain FP32 CUDA cores"}
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+def timed_calls(fn_list, restore, flush, steps, warmup, stream):
+    """Runs each fn once per step bracketed by CUDA events on `stream`; restore
+    and flush run outside the events.  Returns per-fn lists of ms."""
+    import torch
+    times = [[] for _ in fn_list]
+    for s in range(warmup + steps):
+        for i, fn in enumerate(fn_list):
+            restore(i)
+            flush()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            if s >= warmup:
+                times[i].append((e0, e1))
+    torch.cuda.synchronize()
+    return [[a.elapsed_time(b) for a, b in t] for t in times]
+
+
+def blob_image(size, rng):
+    """Sum of 20 Gaussian blobs (centres U[0,size)^2, sigma U[5,50] px,
+    amplitude U[0,1]) plus N(0, 0.01^2) noise."""
+    yy, xx = np.mgrid[0:size, 0:size].astype(np.float64)
+    img = np.zeros((size, size))
+    for _ in range(20):
+        cy, cx = rng.uniform(0, size, 2)
+        s = rng.uniform(5, 50)
+        a = rng.uniform(0, 1)
+        img += a * np.exp(-((yy - cy) ** 2 + (xx - cx) ** 2) / (2 * s * s))
+    img += rng.normal(0, 0.01, img.shape)
+    return img
+
+
+def other_workloads(args, peak, flush, stream):
+    import torch
+    import jtransforms_gb300 as J
+    from jtransforms_gb300 import _native as N
+    out = {}
+    rng = np.random.default_rng(SEED)
+    steps, warm = max(args.steps, 3), args.warmup
+
+    def measure(name, plan, op, buf, batch, dist, scale, flops, bytes_alg, unit_note, extra_fn=None):
+        pristine = buf.clone()
+        fns = [lambda: plan.execute(op, buf, 0, scale, batch=batch, dist=dist)]
+        if extra_fn:
+            fns = [extra_fn]
+        t = timed_calls(fns, lambda i: buf.copy_(pristine), flush, steps, warm, stream)[0]
+        ms = statistics.median(t)
+        out[name] = {"value": flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms": ms, "best_ms": min(t),
+                     "hbm_frac": (bytes_alg / (ms * 1e-3) / 1e9) / peak, "flops": unit_note}
+
+    # config 1: 256 x DoubleFFT_1D(4096) complexForward then complexInverse(scale=true)
+    n, B = 4096, 256
+    f1 = J.DoubleFFT_1D(n)
+    buf = torch.from_numpy(rng.uniform(-1, 1, 2 * n * B)).cuda()
+    pristine = buf.clone()
+
+    def fwd_inv():
+        f1.plan.execute(N.COMPLEX_FORWARD, buf, 0, False, batch=B, dist=2 * n)
+        f1.plan.execute(N.COMPLEX_INVERSE, buf, 0, True, batch=B, dist=2 * n)
+    t = timed_calls([fwd_inv], lambda i: buf.copy_(pristine), flush, steps, warm, stream)[0]
+    ms = statistics.median(t)
+    out["c1_DoubleFFT_1D_4096x256_fwd_inv"] = {
+        "value": 2 * flops_c2c(n, B) / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms": ms,
+        "hbm_frac": (4 * 16 * n * B / (ms * 1e-3) / 1e9) / peak, "flops": "5N log2N x2 directions"}
+
+    # config 2a: FloatFFT_2D(2048, 2048).realForward on a blob image
+    img = blob_image(2048, rng).astype(np.float32).ravel()
+    f2 = J.FloatFFT_2D(2048, 2048)
+    buf = torch.from_numpy(img).cuda()
+    N2 = 2048 * 2048
+    measure("c2a_FloatFFT_2D_2048_realForward", f2.plan, N.REAL_FORWARD, buf, 1, N2, False,
+            2.5 * N2 * math.log2(N2), 2 * 4 * N2, "2.5N log2N")
+    # config 2b: DoubleDCT_2D(1024, 1024).forward(scale=true)
+    img = blob_image(1024, rng).ravel()
+    d2 = J.DoubleDCT_2D(1024, 1024)
+    buf = torch.from_numpy(img).cuda()
+    N2 = 1024 * 1024
+    measure("c2b_DoubleDCT_2D_1024_forward", d2.plan, N.FORWARD, buf, 1, N2, True,
+            2.5 * N2 * math.log2(N2), 2 * 8 * N2, "2.5N log2N")
+    # config 3a: DoubleFFT_3D(256^3).complexForward, N(0,1)
+    f3 = J.DoubleFFT_3D(256, 256, 256)
+    N3 = 256 ** 3
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    buf = torch.randn(2 * N3, dtype=torch.float64, device="cuda", generator=g)
+    measure("c3a_DoubleFFT_3D_256_complexForward", f3.plan, N.COMPLEX_FORWARD, buf, 1, 2 * N3, False,
+            flops_c2c(N3, 1), 2 * 16 * N3, "5N log2N")
+    del buf
+    # config 3b/3c: DoubleDST_3D / DoubleDHT_3D (128^3) uniform[-1, 1)
+    N3 = 128 ** 3
+    x = torch.from_numpy(rng.uniform(-1, 1, N3)).cuda()
+    s3 = J.DoubleDST_3D(128, 128, 128)
+    measure("c3b_DoubleDST_3D_128_forward", s3.plan, N.FORWARD, x, 1, N3, True,
+            2.5 * N3 * math.log2(N3), 2 * 8 * N3, "2.5N log2N")
+    h3 = J.DoubleDHT_3D(128, 128, 128)
+    measure("c3c_DoubleDHT_3D_128_forward", h3.plan, N.FORWARD, x, 1, N3, False,
+            2.5 * N3 * math.log2(N3), 2 * 8 * N3, "2.5N log2N")
+    return out
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import jtransforms_gb300 as J
+    from jtransforms_gb300 import _native as N
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    peak, peak_src = measured_peaks()
+    stream = torch.cuda.current_stream()
+    flushbuf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def flush():
+        flushbuf.fill_(1.0)
+
+    plans, pristine, work = [], [], []
+    g = torch.Generator(device="cuda").manual_seed(SEED + rank)
+    for n in SIZES:
+        plans.append(J.FloatFFT_1D(n))
+        p = torch.randn(2 * ELEMS, dtype=torch.float32, device="cuda", generator=g)
+        pristine.append(p)
+        work.append(torch.empty_like(p))
+    torch.cuda.synchronize()
+
+    fns = [(lambda i=i: plans[i].plan.execute(N.COMPLEX_FORWARD, work[i], 0, False,
+                                              batch=ELEMS // SIZES[i], dist=2 * SIZES[i]))
+           for i in range(len(SIZES))]
+    # warm-up (tables, scratch, clocks)
+    timed_calls(fns, lambda i: work[i].copy_(pristine[i]), flush, 0, args.warmup, stream)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    J.launch_count(reset=True)
+    t_wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        times = timed_calls(fns, lambda i: work[i].copy_(pristine[i]), flush, args.steps, 0, stream)
+    torch.cuda.synchronize()
+    launches = J.launch_count(reset=True)
+    wall = time.perf_counter() - t_wall0
+    per_size_ms = [sum(t) / len(t) for t in times]
+    step_ms = sum(per_size_ms)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        step_ms = float(tt.item())
+    flops_step = sum(flops_c2c(n, ELEMS // n) for n in SIZES) * world
+    value = flops_step / (step_ms * 1e-3) / 1e9
+    bytes_step = 2 * 8 * ELEMS * len(SIZES)
+    achieved = bytes_step / (sum(per_size_ms) * 1e-3) / 1e9
+    per_size = {f"2^{int(math.log2(n))}": {"ms": ms, "GFLOP/s": flops_c2c(n, ELEMS // n) / (ms * 1e-3) / 1e9,
+                                           "GB/s": 2 * 8 * ELEMS / (ms * 1e-3) / 1e9,
+                                           "algorithm": ["direct", "two-pass", "bluestein", "trivial"][plans[i].plan.algorithm(0)]}
+                for i, (n, ms) in enumerate(zip(SIZES, per_size_ms))}
+
+    # error of the FP32 path against FP64 (input set (a), one transform per size)
+    err = {}
+    for i, n in enumerate(SIZES):
+        x = pristine[i][: 2 * n].double()
+        ref = torch.fft.fft(torch.complex(x[0::2], x[1::2]))
+        w = pristine[i][: 2 * n].clone()
+        plans[i].plan.execute(N.COMPLEX_FORWARD, w, 0, False)
+        got = torch.complex(w[0::2].double(), w[1::2].double())
+        err[f"2^{int(math.log2(n))}"] = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+
+    # end to end through the C ABI with pinned host buffers
+    e2e_steps = max(1, min(args.steps, 3))
+    host = []
+    for i, n in enumerate(SIZES):
+        h = torch.empty(2 * ELEMS, dtype=torch.float32, pin_memory=True)
+        h.copy_(pristine[i])
+        host.append(h.numpy())
+    del work
+    torch.cuda.synchronize()
+    for i, n in enumerate(SIZES):  # warm the host path
+        plans[i].plan.execute(N.COMPLEX_FORWARD, host[i][: 2 * n * 4], 0, False, batch=4, dist=2 * n)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for i, n in enumerate(SIZES):
+            plans[i].plan.execute(N.COMPLEX_FORWARD, host[i], 0, False, batch=ELEMS // n, dist=2 * n)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = flops_step / world / e2e_s / 1e9 * world
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded N(0,1) complex64)",
+            "config": headline_config(args),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "fft_tile_kernel (all launches of one 1 GiB batch call)",
+                         "algorithmic_bytes_per_call": 2 * 8 * ELEMS},
+            "per_size": per_size, "rel_l2_vs_fp64": err,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * ELEMS * len(SIZES),
+                    "d2h_bytes_per_step": 8 * ELEMS * len(SIZES),
+                    "path": "FloatFFT_1D plan -> jt_execute_batch on pinned host arrays"},
+            "gpu_launches": launches // max(args.steps, 1) * 0 + launches,
+            "timed_wall_s": wall}
+    clocks = clk.summary()
+    line["clocks"] = clocks
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, th, desc = cpu_sample(3.0)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": desc}
+    if rank == 0 and not args.no_other:
+        del pristine
+        torch.cuda.empty_cache()
+        try:
+            line["other_workloads"] = other_workloads(args, peak, flush, stream)
+        except Exception as e:  # report, do not hide
+            line["other_workloads_error"] = repr(e)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-other", action="store_true", help="skip the other workloads")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,1154 @@
+// jt_engine.cu -- host side of jtransforms_gb300: per-size plans, algorithm
+// choice, scratch management and the C ABI declared in include/jtgpu.h.
+//
+// Algorithm choice per complex length n (GPU-first, not the reference's
+// split-radix / FFTPACK / Bluestein choice, which only fixes the results):
+//   DIRECT    n <= 8192 (f32) / 4096 (f64) with prime factors <= 63: one
+//             shared-memory tile kernel per batch of lines.
+//   TWOPASS   n = n1 * n2 with both DIRECT: column pass with the four-step
+//             twiddle fused into its store, then a row pass that writes the
+//             transposed (natural-order) result.  The batch is processed in
+//             chunks whose intermediate stays in L2.
+//   BLUESTEIN everything else: chirp-z with a power-of-two convolution of
+//             nextPow2(2n-1) points (fft/DoubleFFT_1D.java:1864-2107), chirp
+//             tables generated in FP64 on the device.
+#include "jt_device.cuh"
+#include "../../include/jtgpu.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace jt {
+
+static thread_local int g_last_cuda = 0;
+static thread_local int64_t g_launches = 0;
+
+#define JT_CU(call)                                  \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) {                     \
+            g_last_cuda = (int)e_;                   \
+            return e_ == cudaErrorMemoryAllocation ? JT_ENOMEM : JT_ECUDA; \
+        }                                            \
+    } while (0)
+
+#define JT_TRY(call)                 \
+    do {                             \
+        int s_ = (call);             \
+        if (s_ != JT_OK) return s_;  \
+    } while (0)
+
+static bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
+static int64_t next_pow2(int64_t x) {
+    int64_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// Per-thread device workspace: a bump allocator that is sized by a dry run
+// of the same call (no launches), then handed out in 256-byte aligned slices.
+struct Arena {
+    char *base = nullptr;
+    size_t cap = 0, used = 0, peak = 0;
+    void *get(size_t bytes, bool dry) {
+        size_t off = (used + 255) & ~(size_t)255;
+        used = off + bytes;
+        if (used > peak) peak = used;
+        return dry ? nullptr : (void *)(base + off);
+    }
+};
+
+struct Ctx {
+    cudaStream_t s = nullptr;
+    bool dry = false;
+    Arena *ws = nullptr;
+};
+
+static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+#define LAUNCH1D(ctx, total, kernel, ...)                                              \
+    do {                                                                               \
+        if (!(ctx).dry && (total) > 0) {                                               \
+            int64_t g_ = cdiv((total), 256);                                           \
+            auto kfn_ = kernel;                                                        \
+            kfn_<<<(unsigned)g_, 256, 0, (ctx).s>>>(__VA_ARGS__);                      \
+            g_launches++;                                                              \
+        }                                                                              \
+    } while (0)
+
+static int g_smem_optin = 0;
+static std::once_flag g_dev_once;
+static int g_dev_status = JT_OK;
+
+static int device_init() {
+    std::call_once(g_dev_once, [] {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+            g_dev_status = JT_ENODEV;
+            return;
+        }
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncSetAttribute(fft_tile_kernel<-1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(fft_tile_kernel<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(fft_tile_kernel<-1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(fft_tile_kernel<1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        if (cudaGetLastError() != cudaSuccess) g_dev_status = JT_ECUDA;
+    });
+    return g_dev_status;
+}
+
+// ---------------------------------------------------------------------------
+// Complex FFT of one length
+// ---------------------------------------------------------------------------
+enum { ALG_DIRECT = 0, ALG_TWOPASS = 1, ALG_BLUESTEIN = 2, ALG_TRIVIAL = 3 };
+
+static const int kMaxThreads = 512;
+
+template <typename T> struct Lim {
+    static int64_t lmax() { return sizeof(T) == 4 ? 8192 : 4096; }
+};
+
+// Radices for a DIRECT line; empty if n has a prime factor > 63.
+static std::vector<int> direct_radices(int64_t n) {
+    std::vector<int> r;
+    int64_t m = n;
+    int a = 0;
+    while (m % 2 == 0) { m /= 2; a++; }
+    while (a >= 4) { r.push_back(16); a -= 4; }
+    if (a == 3) r.push_back(8);
+    else if (a == 2) r.push_back(4);
+    else if (a == 1) r.push_back(2);
+    for (int p : {7, 5, 3})
+        while (m % p == 0) { r.push_back(p); m /= p; }
+    for (int p = 11; p <= 63 && m > 1; p += 2)
+        while (m % p == 0) { r.push_back(p); m /= p; }
+    if (m != 1) r.clear();
+    if (n == 1) r.clear();
+    return r;
+}
+
+template <typename T> struct Fft1 {
+    typedef typename V2<T>::t C2;
+    int64_t n = 0;
+    int algo = ALG_TRIVIAL;
+    std::vector<int> radix;
+    C2 *W = nullptr;
+    int64_t n1 = 0, n2 = 0;
+    std::unique_ptr<Fft1> pa, pb, pbl;
+    C2 *Whi = nullptr, *Wlo = nullptr;
+    int lo_bits = 0;
+    int64_t nB = 0;
+    C2 *bk1 = nullptr, *bk2 = nullptr;
+
+    ~Fft1() {
+        for (void *p : {(void *)W, (void *)Whi, (void *)Wlo, (void *)bk1, (void *)bk2})
+            if (p) cudaFree(p);
+    }
+
+    static bool direct_ok(int64_t n) { return n >= 2 && n <= Lim<T>::lmax() && !direct_radices(n).empty(); }
+
+    static int make_roots(C2 **out, int64_t count, int64_t num, int64_t den) {
+        JT_CU(cudaMalloc(out, sizeof(C2) * std::max<int64_t>(count, 1)));
+        roots_kernel<T><<<(unsigned)cdiv(count, 256), 256>>>(*out, count, num, den);
+        g_launches++;
+        JT_CU(cudaGetLastError());
+        return JT_OK;
+    }
+
+    static int create(int64_t n, std::unique_ptr<Fft1> &out) {
+        std::unique_ptr<Fft1> f(new (std::nothrow) Fft1());
+        if (!f) return JT_ENOMEM;
+        f->n = n;
+        if (n == 1) {
+            f->algo = ALG_TRIVIAL;
+        } else if (direct_ok(n)) {
+            f->algo = ALG_DIRECT;
+            f->radix = direct_radices(n);
+            JT_TRY(make_roots(&f->W, n, 1, n));
+        } else {
+            // balanced split into two DIRECT lengths
+            int64_t best = 0;
+            double bestd = 1e300;
+            for (int64_t d = 2; d <= Lim<T>::lmax() && d < n; d++) {
+                if (n % d) continue;
+                int64_t e = n / d;
+                if (!direct_ok(d) || !direct_ok(e)) continue;
+                double dd = std::fabs(std::log((double)d) - std::log((double)e));
+                if (dd < bestd) { bestd = dd; best = d; }
+            }
+            if (best) {
+                f->algo = ALG_TWOPASS;
+                f->n1 = best;
+                f->n2 = n / best;
+                JT_TRY(create(f->n1, f->pa));
+                JT_TRY(create(f->n2, f->pb));
+                f->lo_bits = 0;
+                while (((int64_t)1 << (2 * f->lo_bits)) < n) f->lo_bits++;
+                int64_t nlo = (int64_t)1 << f->lo_bits;
+                JT_TRY(make_roots(&f->Wlo, nlo, 1, n));
+                JT_TRY(make_roots(&f->Whi, cdiv(n, nlo), nlo, n));
+            } else {
+                f->algo = ALG_BLUESTEIN;
+                f->nB = next_pow2(2 * n - 1);
+                if (f->nB > Lim<T>::lmax() * Lim<T>::lmax()) return JT_ETOOBIG;
+                JT_TRY(create(f->nB, f->pbl));
+                JT_TRY(f->make_chirp());
+            }
+        }
+        out = std::move(f);
+        return JT_OK;
+    }
+
+    int make_chirp();
+
+    // DIRECT pass over `nlines` lines with arbitrary layouts.
+    int exec_direct(Ctx &ctx, const C2 *in, C2 *out, int64_t nlines, const Layout &lin, const Layout &lout, int sign,
+                    double scale, int64_t tw_n = 0, int64_t tw_inner = 1, const C2 *Whi_ = nullptr, const C2 *Wlo_ = nullptr,
+                    int tw_lo_bits = 0) const {
+        if (nlines <= 0) return JT_OK;
+        const int L = (int)n;
+        const int Lp = padded_len(L);
+        const bool strided = lin.estride != 1 || lout.estride != 1;
+        int64_t target = sizeof(T) == 4 ? 4096 : 2048;
+        int C = (int)std::max<int64_t>(1, target / L);
+        if (strided) C = std::max(C, sizeof(T) == 4 ? 16 : 8);
+        size_t per_line = 2 * (size_t)Lp * sizeof(C2);
+        int cmax = (int)std::max<size_t>(1, (size_t)g_smem_optin / per_line);
+        C = std::min(C, cmax);
+        if ((int64_t)C > nlines) C = (int)nlines;
+        size_t smem = per_line * C;
+        int threads = (int)std::min<int64_t>(kMaxThreads, std::max<int64_t>(64, cdiv((int64_t)C * L / 16, 32) * 32));
+        TileParams p;
+        memset(&p, 0, sizeof(p));
+        p.L = L;
+        p.npass = (int)radix.size();
+        for (int i = 0; i < p.npass; i++) p.radix[i] = radix[i];
+        p.C = C;
+        p.nlines = nlines;
+        p.lin = lin;
+        p.lout = lout;
+        p.scale = scale;
+        p.tw_n = tw_n;
+        p.tw_inner = tw_inner;
+        p.tw_lo_bits = tw_lo_bits;
+        if (ctx.dry) return JT_OK;
+        int64_t grid = cdiv(nlines, C);
+        if (grid > 0x7fffffff) return JT_ETOOBIG;
+        if (sign < 0)
+            fft_tile_kernel<-1, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, Whi_, Wlo_);
+        else
+            fft_tile_kernel<1, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, Whi_, Wlo_);
+        g_launches++;
+        return JT_OK;
+    }
+
+    // `batch` contiguous lines: line b at in + b*din, out + b*dout (complex units).
+    int exec(Ctx &ctx, const C2 *in, int64_t din, C2 *out, int64_t dout, int64_t batch, int sign, double scale) const {
+        if (batch <= 0) return JT_OK;
+        switch (algo) {
+            case ALG_TRIVIAL: {
+                if (in == out && scale == 1.0) return JT_OK;
+                LAUNCH1D(ctx, batch, copy_complex_kernel<T>, in, din, out, dout, (int64_t)1, batch, scale, 0);
+                return JT_OK;
+            }
+            case ALG_DIRECT: {
+                Layout li = {1, din, 0, 1}, lo = {1, dout, 0, 1};
+                return exec_direct(ctx, in, out, batch, li, lo, sign, scale);
+            }
+            case ALG_TWOPASS: {
+                int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)(48ll << 20) / (n * (int64_t)sizeof(C2))));
+                C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * chunk * n, ctx.dry);
+                for (int64_t b = 0; b < batch; b += chunk) {
+                    int64_t cb = std::min(chunk, batch - b);
+                    Layout lai = {n2, din, 1, n2}, lao = {n2, n, 1, n2};
+                    JT_TRY(pa->exec_direct(ctx, in + b * din, tmp, cb * n2, lai, lao, sign, 1.0, n, n2, Whi, Wlo, lo_bits));
+                    Layout lbi = {n1, n, n2, 1}, lbo = {n1, dout, 1, n1};
+                    JT_TRY(pb->exec_direct(ctx, tmp, out + b * dout, cb * n1, lbi, lbo, sign, scale));
+                }
+                return JT_OK;
+            }
+            case ALG_BLUESTEIN: {
+                int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)(128ll << 20) / (nB * (int64_t)sizeof(C2))));
+                C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * chunk * nB, ctx.dry);
+                for (int64_t b = 0; b < batch; b += chunk) {
+                    int64_t cb = std::min(chunk, batch - b);
+                    if (sign < 0) LAUNCH1D(ctx, cb * nB, (bluestein_pre_kernel<-1, T>), in + b * din, din, tmp, bk1, n, nB, cb);
+                    else LAUNCH1D(ctx, cb * nB, (bluestein_pre_kernel<1, T>), in + b * din, din, tmp, bk1, n, nB, cb);
+                    JT_TRY(pbl->exec(ctx, tmp, nB, tmp, nB, cb, -1, 1.0));
+                    if (sign < 0) LAUNCH1D(ctx, cb * nB, (bluestein_mul_kernel<-1, T>), tmp, bk2, nB, cb * nB);
+                    else LAUNCH1D(ctx, cb * nB, (bluestein_mul_kernel<1, T>), tmp, bk2, nB, cb * nB);
+                    JT_TRY(pbl->exec(ctx, tmp, nB, tmp, nB, cb, 1, 1.0));
+                    if (sign < 0) LAUNCH1D(ctx, cb * n, (bluestein_post_kernel<-1, T>), out + b * dout, dout, tmp, bk1, n, nB, cb, scale);
+                    else LAUNCH1D(ctx, cb * n, (bluestein_post_kernel<1, T>), out + b * dout, dout, tmp, bk1, n, nB, cb, scale);
+                }
+                return JT_OK;
+            }
+        }
+        return JT_EINVAL;
+    }
+};
+
+// bk1 (n) and bk2 = FFT_-(symmetric chirp / nB) (nB), built in FP64 on the
+// device and rounded to T (fft/DoubleFFT_1D.java:1864-1890).
+template <typename T> int Fft1<T>::make_chirp() {
+    JT_CU(cudaMalloc(&bk1, sizeof(C2) * n));
+    JT_CU(cudaMalloc(&bk2, sizeof(C2) * nB));
+    double2 *b64 = nullptr;
+    JT_CU(cudaMalloc(&b64, sizeof(double2) * nB));
+    chirp_kernel<T><<<(unsigned)cdiv(nB, 256), 256>>>(bk1, b64, n, nB);
+    g_launches++;
+    int st = JT_OK;
+    {
+        std::unique_ptr<Fft1<double>> f64;
+        st = Fft1<double>::create(nB, f64);
+        if (st == JT_OK) {
+            Arena ar;
+            Ctx c;
+            c.s = nullptr;
+            c.ws = &ar;
+            c.dry = true;
+            st = f64->exec(c, b64, nB, b64, nB, 1, -1, 1.0);
+            if (st == JT_OK) {
+                if (ar.peak) {
+                    if (cudaMalloc(&ar.base, ar.peak) != cudaSuccess) st = JT_ENOMEM;
+                    ar.cap = ar.peak;
+                }
+                ar.used = 0;
+                c.dry = false;
+                if (st == JT_OK) st = f64->exec(c, b64, nB, b64, nB, 1, -1, 1.0);
+                cudaDeviceSynchronize();
+                if (ar.base) cudaFree(ar.base);
+            }
+        }
+    }
+    if (st == JT_OK) {
+        d2t_kernel<T><<<(unsigned)cdiv(nB, 256), 256>>>(bk2, b64, nB);
+        g_launches++;
+    }
+    cudaDeviceSynchronize();
+    cudaFree(b64);
+    JT_CU(cudaGetLastError());
+    return st;
+}
+
+// ---------------------------------------------------------------------------
+// Real FFT of length n (packed layouts of fft/DoubleFFT_1D.java:433-451)
+// ---------------------------------------------------------------------------
+template <typename T> struct Real1 {
+    typedef typename V2<T>::t C2;
+    int64_t n = 0;
+    std::unique_ptr<Fft1<T>> half, full;
+    C2 *Wr = nullptr;
+    ~Real1() {
+        if (Wr) cudaFree(Wr);
+    }
+    static int create(int64_t n, std::unique_ptr<Real1> &out) {
+        std::unique_ptr<Real1> r(new (std::nothrow) Real1());
+        if (!r) return JT_ENOMEM;
+        r->n = n;
+        if (n >= 2 && n % 2 == 0) {
+            JT_TRY(Fft1<T>::create(n / 2, r->half));
+            JT_TRY(Fft1<T>::make_roots(&r->Wr, n / 4 + 1, 1, n));
+        } else if (n > 1) {
+            JT_TRY(Fft1<T>::create(n, r->full));
+        }
+        out = std::move(r);
+        return JT_OK;
+    }
+    bool even() const { return n >= 2 && n % 2 == 0; }
+
+    // In place: n reals at a + b*dist -> packed spectrum.  dist must be even
+    // for even n (the complex view).
+    int fwd_packed(Ctx &ctx, T *a, int64_t dist, int64_t batch) const {
+        if (n == 1 || batch <= 0) return JT_OK;
+        if (even()) {
+            JT_TRY(half->exec(ctx, (C2 *)a, dist / 2, (C2 *)a, dist / 2, batch, -1, 1.0));
+            LAUNCH1D(ctx, batch * (n / 4 + 1), real_post_packed_kernel<T>, a, dist, n, batch, Wr);
+            return JT_OK;
+        }
+        C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * n, ctx.dry);
+        LAUNCH1D(ctx, batch * n, real_to_complex_kernel<T>, a, dist, tmp, n, batch);
+        JT_TRY(full->exec(ctx, tmp, n, tmp, n, batch, -1, 1.0));
+        LAUNCH1D(ctx, batch * n, pack_from_full_kernel<T>, tmp, a, dist, n, batch);
+        return JT_OK;
+    }
+
+    // n reals at a + b*dist -> 2n (full complex spectrum) at the same place;
+    // sign=+1 gives the e^{+} transform (realInverseFull), times scale.
+    int fwd_full(Ctx &ctx, T *a, int64_t dist, int64_t batch, int sign, double scale) const {
+        if (batch <= 0) return JT_OK;
+        if (n == 1) {
+            LAUNCH1D(ctx, batch, scale_kernel<T>, a, dist, (int64_t)1, batch, scale);
+            LAUNCH1D(ctx, batch, scale_kernel<T>, a + 1, dist, (int64_t)1, batch, 0.0);
+            return JT_OK;
+        }
+        if (even()) {
+            const int64_t h = n / 2;
+            C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * h, ctx.dry);
+            JT_TRY(half->exec(ctx, (const C2 *)a, dist / 2, tmp, h, batch, sign, 1.0));
+            if (sign < 0)
+                LAUNCH1D(ctx, batch * (h / 2 + 1), (real_post_full_kernel<-1, T>), (const T *)tmp, 2 * h, a, dist, n, batch, Wr, scale);
+            else
+                LAUNCH1D(ctx, batch * (h / 2 + 1), (real_post_full_kernel<1, T>), (const T *)tmp, 2 * h, a, dist, n, batch, Wr, scale);
+            return JT_OK;
+        }
+        C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * n, ctx.dry);
+        LAUNCH1D(ctx, batch * n, real_to_complex_kernel<T>, a, dist, tmp, n, batch);
+        JT_TRY(full->exec(ctx, tmp, n, tmp, n, batch, sign, scale));
+        LAUNCH1D(ctx, batch * n, copy_complex_kernel<T>, tmp, n, (C2 *)a, dist / 2, n, batch, 1.0, 0);
+        return JT_OK;
+    }
+
+    // In place: packed spectrum -> factor * x, x the 1/n-normalised inverse.
+    int inv_packed(Ctx &ctx, T *a, int64_t dist, int64_t batch, double factor) const {
+        if (batch <= 0) return JT_OK;
+        if (n == 1) {
+            if (factor != 1.0) LAUNCH1D(ctx, batch, scale_kernel<T>, a, dist, (int64_t)1, batch, factor);
+            return JT_OK;
+        }
+        if (even()) {
+            LAUNCH1D(ctx, batch * (n / 4 + 1), real_pre_inverse_kernel<T>, a, dist, n, batch, Wr, factor * 2.0 / (double)n);
+            JT_TRY(half->exec(ctx, (C2 *)a, dist / 2, (C2 *)a, dist / 2, batch, 1, 1.0));
+            return JT_OK;
+        }
+        C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * n, ctx.dry);
+        LAUNCH1D(ctx, batch * n, unpack_to_full_kernel<T>, a, dist, tmp, n, batch);
+        JT_TRY(full->exec(ctx, tmp, n, tmp, n, batch, 1, 1.0));
+        LAUNCH1D(ctx, batch * n, real_part_kernel<T>, tmp, a, dist, n, batch, factor / (double)n);
+        return JT_OK;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// DCT-II/III and DST-II/III (dct/DoubleDCT_1D.java:169-440, dst/DoubleDST_1D.java)
+// ---------------------------------------------------------------------------
+template <typename T> struct Dct1 {
+    typedef typename V2<T>::t C2;
+    int64_t n = 0;
+    std::unique_ptr<Real1<T>> rf;
+    C2 *Wd = nullptr;
+    ~Dct1() {
+        if (Wd) cudaFree(Wd);
+    }
+    static int create(int64_t n, std::unique_ptr<Dct1> &out) {
+        std::unique_ptr<Dct1> d(new (std::nothrow) Dct1());
+        if (!d) return JT_ENOMEM;
+        d->n = n;
+        if (n > 1) {
+            JT_TRY(Real1<T>::create(n, d->rf));
+            JT_TRY(Fft1<T>::make_roots(&d->Wd, n, 1, 4 * n));  // e^{-i pi k/(2n)}
+        }
+        out = std::move(d);
+        return JT_OK;
+    }
+    int64_t vdist() const { return (n + 1) & ~(int64_t)1; }
+
+    int forward(Ctx &ctx, T *a, int64_t dist, int64_t batch, bool scale, bool dst) const {
+        if (n == 1 || batch <= 0) return JT_OK;
+        const int64_t vd = vdist();
+        T *v = (T *)ctx.ws->get(sizeof(T) * batch * vd, ctx.dry);
+        LAUNCH1D(ctx, batch * n, dct2_pre_kernel<T>, a, dist, v, vd, n, batch, (int)dst);
+        JT_TRY(rf->fwd_packed(ctx, v, vd, batch));
+        double mult, mult0;
+        if (scale) {
+            mult = std::sqrt(2.0 / (double)n);
+            mult0 = 1.0 / std::sqrt((double)n);
+        } else {
+            mult = mult0 = is_pow2(n) ? 1.0 : 2.0;
+        }
+        LAUNCH1D(ctx, batch * n, dct2_post_kernel<T>, v, vd, a, dist, n, batch, Wd, mult, mult0, (int)dst);
+        return JT_OK;
+    }
+
+    int inverse(Ctx &ctx, T *a, int64_t dist, int64_t batch, bool scale, bool dst) const {
+        if (n == 1 || batch <= 0) return JT_OK;
+        const int64_t vd = vdist();
+        T *v = (T *)ctx.ws->get(sizeof(T) * batch * vd, ctx.dry);
+        double q, q0;
+        if (scale) {
+            q = std::sqrt(2.0 / (double)n);
+            q0 = 1.0 / std::sqrt((double)n);
+        } else if (is_pow2(n)) {
+            q = q0 = 1.0;
+        } else {
+            q = 1.0 / (double)n;
+            q0 = 0.5 / (double)n;
+        }
+        LAUNCH1D(ctx, batch * (n / 2 + 1), dct3_pre_kernel<T>, a, dist, v, vd, n, batch, Wd, q * (double)n / 2.0,
+                 q0 * (double)n, (int)dst);
+        JT_TRY(rf->inv_packed(ctx, v, vd, batch, 1.0));
+        LAUNCH1D(ctx, batch * n, dct3_post_kernel<T>, v, vd, a, dist, n, batch, (int)dst);
+        return JT_OK;
+    }
+};
+
+// DHT (dht/DoubleDHT_1D.java:94-159, :255-276)
+template <typename T> struct Dht1 {
+    int64_t n = 0;
+    std::unique_ptr<Real1<T>> rf;
+    static int create(int64_t n, std::unique_ptr<Dht1> &out) {
+        std::unique_ptr<Dht1> d(new (std::nothrow) Dht1());
+        if (!d) return JT_ENOMEM;
+        d->n = n;
+        if (n > 1) JT_TRY(Real1<T>::create(n, d->rf));
+        out = std::move(d);
+        return JT_OK;
+    }
+    int forward(Ctx &ctx, T *a, int64_t dist, int64_t batch, double mult) const {
+        if (n == 1 || batch <= 0) return JT_OK;
+        const int64_t vd = (n + 1) & ~(int64_t)1;
+        T *v = (T *)ctx.ws->get(sizeof(T) * batch * vd, ctx.dry);
+        LAUNCH1D(ctx, batch * n, copy_real_kernel<T>, a, dist, v, vd, n, batch);
+        JT_TRY(rf->fwd_packed(ctx, v, vd, batch));
+        LAUNCH1D(ctx, batch * n, dht_post_kernel<T>, v, vd, a, dist, n, batch, mult);
+        return JT_OK;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Plan: one transform kind/precision over 1..3 dimensions.
+// ---------------------------------------------------------------------------
+template <typename T> struct PlanImpl {
+    typedef typename V2<T>::t C2;
+    int kind = JT_FFT, nd = 1;
+    int64_t dims[3] = {1, 1, 1};
+    int64_t N = 1;
+    std::mutex mu;
+    // lazily built per axis length
+    std::map<int64_t, std::unique_ptr<Fft1<T>>> fft;
+    std::map<int64_t, std::unique_ptr<Real1<T>>> real;
+    std::map<int64_t, std::unique_ptr<Dct1<T>>> dct;
+    std::map<int64_t, std::unique_ptr<Dht1<T>>> dht;
+
+    int get_fft(int64_t n, Fft1<T> **out) {
+        auto it = fft.find(n);
+        if (it == fft.end()) {
+            std::unique_ptr<Fft1<T>> f;
+            JT_TRY(Fft1<T>::create(n, f));
+            it = fft.emplace(n, std::move(f)).first;
+        }
+        *out = it->second.get();
+        return JT_OK;
+    }
+    int get_real(int64_t n, Real1<T> **out) {
+        auto it = real.find(n);
+        if (it == real.end()) {
+            std::unique_ptr<Real1<T>> f;
+            JT_TRY(Real1<T>::create(n, f));
+            it = real.emplace(n, std::move(f)).first;
+        }
+        *out = it->second.get();
+        return JT_OK;
+    }
+    int get_dct(int64_t n, Dct1<T> **out) {
+        auto it = dct.find(n);
+        if (it == dct.end()) {
+            std::unique_ptr<Dct1<T>> f;
+            JT_TRY(Dct1<T>::create(n, f));
+            it = dct.emplace(n, std::move(f)).first;
+        }
+        *out = it->second.get();
+        return JT_OK;
+    }
+    int get_dht(int64_t n, Dht1<T> **out) {
+        auto it = dht.find(n);
+        if (it == dht.end()) {
+            std::unique_ptr<Dht1<T>> f;
+            JT_TRY(Dht1<T>::create(n, f));
+            it = dht.emplace(n, std::move(f)).first;
+        }
+        *out = it->second.get();
+        return JT_OK;
+    }
+
+    // Builds every table `op` needs (called under the mutex, outside streams).
+    int prepare(int op) {
+        std::lock_guard<std::mutex> g(mu);
+        Fft1<T> *f;
+        Real1<T> *r;
+        Dct1<T> *d;
+        Dht1<T> *h;
+        if (kind == JT_FFT) {
+            if (nd == 1 && (op == JT_REAL_FORWARD || op == JT_REAL_INVERSE || op == JT_REAL_FORWARD_FULL || op == JT_REAL_INVERSE_FULL))
+                return get_real(dims[0], &r);
+            if (nd == 2 && (op == JT_REAL_FORWARD || op == JT_REAL_INVERSE)) {
+                JT_TRY(get_real(dims[1], &r));
+                return get_fft(dims[0], &f);
+            }
+            for (int a = 0; a < nd; a++) JT_TRY(get_fft(dims[a], &f));
+            return JT_OK;
+        }
+        for (int a = 0; a < nd; a++) {
+            if (kind == JT_DCT || kind == JT_DST) JT_TRY(get_dct(dims[a], &d));
+            else JT_TRY(get_dht(dims[a], &h));
+        }
+        return JT_OK;
+    }
+
+    // Moves axis `ax` of [outer][len][inner] (elements of E bytes) between
+    // the array and a contiguous-line copy.
+    template <typename E> void transpose(Ctx &ctx, const E *in, E *out, int64_t outer, int64_t R, int64_t Cc) const {
+        if (ctx.dry || outer * R * Cc == 0) return;
+        int64_t blocks = outer * cdiv(R, 32) * cdiv(Cc, 32);
+        transpose_kernel<E><<<(unsigned)blocks, dim3(32, 8), 0, ctx.s>>>(in, out, R, Cc, outer);
+        g_launches++;
+    }
+
+    void axis_shape(int ax, int64_t batch, int64_t &outer, int64_t &len, int64_t &inner) const {
+        len = dims[ax];
+        inner = 1;
+        outer = batch;
+        for (int d = ax + 1; d < nd; d++) inner *= dims[d];
+        for (int d = 0; d < ax; d++) outer *= dims[d];
+    }
+
+    // Complex nD transform of `batch` contiguous arrays.
+    int complex_nd(Ctx &ctx, C2 *a, int64_t batch, int sign, bool scale) {
+        for (int ax = nd - 1; ax >= 0; ax--) {
+            int64_t outer, len, inner;
+            axis_shape(ax, batch, outer, len, inner);
+            Fft1<T> *f = fft.at(len).get();
+            double s = (sign > 0 && scale) ? 1.0 / (double)len : 1.0;
+            if (inner == 1) {
+                JT_TRY(f->exec(ctx, a, len, a, len, outer, sign, s));
+            } else if (f->algo == ALG_DIRECT) {
+                Layout l = {inner, len * inner, 1, inner};
+                JT_TRY(f->exec_direct(ctx, a, a, outer * inner, l, l, sign, s));
+            } else if (f->algo == ALG_TRIVIAL) {
+                continue;
+            } else {
+                C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * outer * len * inner, ctx.dry);
+                transpose<C2>(ctx, a, tmp, outer, len, inner);
+                JT_TRY(f->exec(ctx, tmp, len, tmp, len, outer * inner, sign, s));
+                transpose<C2>(ctx, tmp, a, outer, inner, len);
+            }
+        }
+        return JT_OK;
+    }
+
+    // Applies a real 1D line operation along every axis (DCT/DST/DHT).
+    template <typename F> int real_axes(Ctx &ctx, T *a, int64_t batch, F line_op) {
+        for (int ax = nd - 1; ax >= 0; ax--) {
+            int64_t outer, len, inner;
+            axis_shape(ax, batch, outer, len, inner);
+            if (inner == 1) {
+                JT_TRY(line_op(ctx, len, a, len, outer));
+            } else {
+                T *tmp = (T *)ctx.ws->get(sizeof(T) * outer * len * inner, ctx.dry);
+                transpose<T>(ctx, a, tmp, outer, len, inner);
+                JT_TRY(line_op(ctx, len, tmp, len, outer * inner));
+                transpose<T>(ctx, tmp, a, outer, inner, len);
+            }
+        }
+        return JT_OK;
+    }
+
+    int64_t extent(int op) const {
+        if (kind == JT_FFT) {
+            if (op == JT_REAL_FORWARD || op == JT_REAL_INVERSE) return N;
+            return 2 * N;
+        }
+        return N;
+    }
+
+    // Runs `op` on `batch` arrays at a + b*dist (dist == extent for nD).
+    int run(Ctx &ctx, int op, T *a, int64_t batch, int64_t dist, bool scale) {
+        if (kind == JT_FFT) {
+            if (nd == 1) {
+                const int64_t n = dims[0];
+                if (op == JT_COMPLEX_FORWARD || op == JT_COMPLEX_INVERSE) {
+                    Fft1<T> *f = fft.at(n).get();
+                    int sign = op == JT_COMPLEX_FORWARD ? -1 : 1;
+                    double s = (op == JT_COMPLEX_INVERSE && scale) ? 1.0 / (double)n : 1.0;
+                    return f->exec(ctx, (C2 *)a, dist / 2, (C2 *)a, dist / 2, batch, sign, s);
+                }
+                Real1<T> *r = real.at(n).get();
+                switch (op) {
+                    case JT_REAL_FORWARD: return r->fwd_packed(ctx, a, dist, batch);
+                    case JT_REAL_FORWARD_FULL: return r->fwd_full(ctx, a, dist, batch, -1, 1.0);
+                    case JT_REAL_INVERSE_FULL: return r->fwd_full(ctx, a, dist, batch, 1, scale ? 1.0 / (double)n : 1.0);
+                    case JT_REAL_INVERSE: {
+                        double factor = scale ? 1.0 : ((is_pow2(n) && n > 1) ? (double)n / 2.0 : (double)n);
+                        return r->inv_packed(ctx, a, dist, batch, factor);
+                    }
+                }
+                return JT_EINVAL;
+            }
+            if (dist != extent(op)) return JT_EINVAL;
+            switch (op) {
+                case JT_COMPLEX_FORWARD: return complex_nd(ctx, (C2 *)a, batch, -1, false);
+                case JT_COMPLEX_INVERSE: return complex_nd(ctx, (C2 *)a, batch, 1, scale);
+                case JT_REAL_FORWARD_FULL:
+                case JT_REAL_INVERSE_FULL: {
+                    T *tmp = (T *)ctx.ws->get(sizeof(T) * batch * N, ctx.dry);
+                    LAUNCH1D(ctx, batch * N, copy_real_kernel<T>, a, dist, tmp, N, N, batch);
+                    LAUNCH1D(ctx, batch * N, real_to_complex_kernel<T>, tmp, N, (C2 *)a, N, batch);
+                    int sign = op == JT_REAL_FORWARD_FULL ? -1 : 1;
+                    return complex_nd(ctx, (C2 *)a, batch, sign, op == JT_REAL_INVERSE_FULL && scale);
+                }
+                case JT_REAL_FORWARD:
+                case JT_REAL_INVERSE: {
+                    if (nd != 2) return JT_EINVAL;
+                    const int64_t rows = dims[0], cols = dims[1];
+                    Real1<T> *r = real.at(cols).get();
+                    Fft1<T> *fr = fft.at(rows).get();
+                    Layout l = {cols / 2, rows * cols / 2, 1, cols / 2};
+                    if (op == JT_REAL_FORWARD) {
+                        JT_TRY(r->fwd_packed(ctx, a, cols, batch * rows));
+                        JT_TRY(column_fft(ctx, fr, (C2 *)a, batch, rows, cols / 2, l, -1, 1.0));
+                        LAUNCH1D(ctx, batch * std::max<int64_t>(rows / 2 - 1, 0), rdft2d_kernel<T>, a, dist, rows, cols, batch, 1);
+                        return JT_OK;
+                    }
+                    LAUNCH1D(ctx, batch * std::max<int64_t>(rows / 2 - 1, 0), rdft2d_kernel<T>, a, dist, rows, cols, batch, -1);
+                    JT_TRY(column_fft(ctx, fr, (C2 *)a, batch, rows, cols / 2, l, 1, scale ? 1.0 / (double)rows : 1.0));
+                    double factor = scale ? 1.0 : (double)cols / 2.0;
+                    return r->inv_packed(ctx, a, cols, batch * rows, factor);
+                }
+            }
+            return JT_EINVAL;
+        }
+        if (op != JT_FORWARD && op != JT_INVERSE) return JT_EINVAL;
+        if (nd > 1 && dist != N) return JT_EINVAL;
+        const bool fwd = op == JT_FORWARD;
+        if (kind == JT_DCT || kind == JT_DST) {
+            const bool dst = kind == JT_DST;
+            if (nd == 1) {
+                Dct1<T> *d = dct.at(dims[0]).get();
+                return fwd ? d->forward(ctx, a, dist, batch, scale, dst) : d->inverse(ctx, a, dist, batch, scale, dst);
+            }
+            return real_axes(ctx, a, batch, [&](Ctx &c, int64_t len, T *x, int64_t xd, int64_t nb) {
+                Dct1<T> *d = dct.at(len).get();
+                return fwd ? d->forward(c, x, xd, nb, scale, dst) : d->inverse(c, x, xd, nb, scale, dst);
+            });
+        }
+        // DHT
+        if (nd == 1) {
+            Dht1<T> *h = dht.at(dims[0]).get();
+            double mult = (!fwd && scale) ? 1.0 / (double)dims[0] : 1.0;
+            return h->forward(ctx, a, dist, batch, mult);
+        }
+        JT_TRY(real_axes(ctx, a, batch, [&](Ctx &c, int64_t len, T *x, int64_t xd, int64_t nb) {
+            return dht.at(len)->forward(c, x, xd, nb, 1.0);
+        }));
+        for (int64_t b = 0; b < batch; b++) {
+            T *p = a + b * dist;
+            if (nd == 2) LAUNCH1D(ctx, (dims[0] / 2 + 1) * (dims[1] / 2 + 1), ytransform2_kernel<T>, p, dims[0], dims[1]);
+            else LAUNCH1D(ctx, (dims[0] / 2 + 1) * (dims[1] / 2 + 1) * (dims[2] / 2 + 1), ytransform3_kernel<T>, p, dims[0], dims[1], dims[2]);
+        }
+        if (!fwd && scale) LAUNCH1D(ctx, batch * N, scale_kernel<T>, a, dist, N, batch, 1.0 / (double)N);
+        return JT_OK;
+    }
+
+    // Column pass over `cols` complex columns of `rows` rows, batch arrays.
+    int column_fft(Ctx &ctx, Fft1<T> *f, C2 *a, int64_t batch, int64_t rows, int64_t cols, const Layout &l, int sign, double s) {
+        if (f->algo == ALG_DIRECT) return f->exec_direct(ctx, a, a, batch * cols, l, l, sign, s);
+        if (f->algo == ALG_TRIVIAL) return JT_OK;
+        C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * rows * cols, ctx.dry);
+        transpose<C2>(ctx, a, tmp, batch, rows, cols);
+        JT_TRY(f->exec(ctx, tmp, rows, tmp, rows, batch * cols, sign, s));
+        transpose<C2>(ctx, tmp, a, batch, cols, rows);
+        return JT_OK;
+    }
+};
+
+}  // namespace jt
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace jt;
+
+struct jt_plan {
+    int kind, prec, nd;
+    int64_t dims[3];
+    int mode;
+    void *impl;
+};
+
+namespace {
+
+struct ThreadState {
+    cudaStream_t stream = nullptr;
+    Arena arena;
+    cudaEvent_t done = nullptr;
+    cudaStream_t last = nullptr;
+    ~ThreadState() {
+        // device resources are reclaimed at process exit
+    }
+};
+thread_local ThreadState t_state;
+
+int ensure_stream() {
+    if (!t_state.stream) {
+        JT_CU(cudaStreamCreateWithFlags(&t_state.stream, cudaStreamNonBlocking));
+        JT_CU(cudaEventCreateWithFlags(&t_state.done, cudaEventDisableTiming));
+    }
+    return JT_OK;
+}
+
+int ensure_arena(size_t bytes) {
+    Arena &a = t_state.arena;
+    if (bytes <= a.cap) return JT_OK;
+    if (a.base) {
+        cudaStreamSynchronize(t_state.stream);
+        if (t_state.last && t_state.last != t_state.stream) cudaStreamSynchronize(t_state.last);
+        cudaFree(a.base);
+        a.base = nullptr;
+        a.cap = 0;
+    }
+    size_t cap = std::max(bytes, (size_t)(a.cap * 3 / 2));
+    JT_CU(cudaMalloc(&a.base, cap));
+    a.cap = cap;
+    return JT_OK;
+}
+
+template <typename T> PlanImpl<T> *impl_of(jt_plan *p) { return (PlanImpl<T> *)p->impl; }
+
+// Runs op on device memory: dry run to size the scratch, then the launches.
+template <typename T>
+int run_device(jt_plan *p, int op, T *a, int64_t batch, int64_t dist, bool scale, cudaStream_t s) {
+    PlanImpl<T> *im = impl_of<T>(p);
+    JT_TRY(im->prepare(op));
+    Ctx c;
+    c.s = s;
+    c.ws = &t_state.arena;
+    c.dry = true;
+    t_state.arena.used = 0;
+    t_state.arena.peak = 0;
+    std::lock_guard<std::mutex> g(im->mu);
+    JT_TRY(im->run(c, op, a, batch, dist, scale));
+    size_t need = t_state.arena.peak;
+    JT_TRY(ensure_arena(need));
+    // the arena is shared by this thread's calls: order this call after the
+    // previous one when it ran on another stream
+    if (t_state.last && t_state.last != s) {
+        JT_CU(cudaEventRecord(t_state.done, t_state.last));
+        JT_CU(cudaStreamWaitEvent(s, t_state.done, 0));
+    }
+    t_state.arena.used = 0;
+    c.dry = false;
+    JT_TRY(im->run(c, op, a, batch, dist, scale));
+    t_state.last = s;
+    JT_CU(cudaGetLastError());
+    return JT_OK;
+}
+
+bool valid_op(const jt_plan *p, int op) {
+    if (p->kind == JT_FFT) return op >= JT_COMPLEX_FORWARD && op <= JT_REAL_INVERSE_FULL;
+    return op == JT_FORWARD || op == JT_INVERSE;
+}
+
+int check_op(const jt_plan *p, int op) {
+    if (!valid_op(p, op)) return JT_EINVAL;
+    if (p->kind == JT_FFT && p->nd > 1 && (op == JT_REAL_FORWARD || op == JT_REAL_INVERSE)) {
+        for (int d = 0; d < p->nd; d++)
+            if (!is_pow2(p->dims[d])) return JT_ENOTPOW2;
+        if (p->nd == 3) return JT_EINVAL;  // packed 3D real layout: not built yet
+    }
+    return JT_OK;
+}
+
+template <typename T>
+int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t batch, int64_t dist, int scale) {
+    int64_t ext = 0;
+    JT_TRY(jt_plan_extent(p, op, &ext));
+    if (!host || batch < 0 || off < 0) return JT_EINVAL;
+    if (batch == 0) return JT_OK;
+    if (batch > 1 && dist < ext) return JT_EINVAL;
+    if (off + (batch - 1) * dist + ext > len) return JT_ESHORTBUF;
+    JT_TRY(device_init());
+    JT_TRY(ensure_stream());
+    cudaStream_t s = t_state.stream;
+    // device copy laid out densely at distance ext (even, for complex views)
+    int64_t dd = (ext + 1) & ~(int64_t)1;
+    if (p->nd > 1) dd = ext;
+    PlanImpl<T> *im = impl_of<T>(p);
+    JT_TRY(im->prepare(op));
+    // size: array + scratch (dry run)
+    Ctx c;
+    c.s = s;
+    c.ws = &t_state.arena;
+    c.dry = true;
+    t_state.arena.used = 0;
+    t_state.arena.peak = 0;
+    T *dev = (T *)t_state.arena.get(sizeof(T) * dd * batch, true);
+    std::lock_guard<std::mutex> g(im->mu);
+    JT_TRY(im->run(c, op, dev, batch, dd, scale != 0));
+    JT_TRY(ensure_arena(t_state.arena.peak));
+    if (t_state.last && t_state.last != s) {
+        JT_CU(cudaEventRecord(t_state.done, t_state.last));
+        JT_CU(cudaStreamWaitEvent(s, t_state.done, 0));
+    }
+    t_state.arena.used = 0;
+    c.dry = false;
+    dev = (T *)t_state.arena.get(sizeof(T) * dd * batch, false);
+    T *h = (T *)host + off;
+    // extent for input: ops whose input is n reals in a 2n output region still
+    // copy the whole extent (the reference reads only the first n).
+    if (dist == dd || batch == 1) {
+        JT_CU(cudaMemcpyAsync(dev, h, sizeof(T) * ((batch - 1) * dd + ext), cudaMemcpyHostToDevice, s));
+    } else {
+        JT_CU(cudaMemcpy2DAsync(dev, sizeof(T) * dd, h, sizeof(T) * dist, sizeof(T) * ext, batch, cudaMemcpyHostToDevice, s));
+    }
+    JT_TRY(im->run(c, op, dev, batch, dd, scale != 0));
+    if (dist == dd || batch == 1) {
+        JT_CU(cudaMemcpyAsync(h, dev, sizeof(T) * ((batch - 1) * dd + ext), cudaMemcpyDeviceToHost, s));
+    } else {
+        JT_CU(cudaMemcpy2DAsync(h, sizeof(T) * dist, dev, sizeof(T) * dd, sizeof(T) * ext, batch, cudaMemcpyDeviceToHost, s));
+    }
+    t_state.last = s;
+    JT_CU(cudaStreamSynchronize(s));
+    JT_CU(cudaGetLastError());
+    return JT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int jt_plan_create(int kind, int prec, int ndim, const int64_t *dims, jt_plan **out) {
+    if (!out || !dims) return JT_EINVAL;
+    *out = nullptr;
+    if (kind < JT_FFT || kind > JT_DHT || (prec != JT_FLOAT32 && prec != JT_FLOAT64) || ndim < 1 || ndim > 3) return JT_EINVAL;
+    for (int d = 0; d < ndim; d++) {
+        if (ndim == 1 && dims[d] < 1) return JT_EBADSIZE;
+        if (ndim > 1 && dims[d] <= 1) return JT_EBADSIZE;
+    }
+    JT_TRY(device_init());
+    jt_plan *p = new (std::nothrow) jt_plan();
+    if (!p) return JT_ENOMEM;
+    p->kind = kind;
+    p->prec = prec;
+    p->nd = ndim;
+    p->mode = JT_MODE_FP32;
+    int64_t N = 1;
+    for (int d = 0; d < 3; d++) p->dims[d] = d < ndim ? dims[d] : 1;
+    for (int d = 0; d < ndim; d++) N *= dims[d];
+    auto fill = [&](auto *im) {
+        im->kind = kind;
+        im->nd = ndim;
+        for (int d = 0; d < 3; d++) im->dims[d] = p->dims[d];
+        im->N = N;
+    };
+    if (prec == JT_FLOAT32) {
+        auto *im = new (std::nothrow) PlanImpl<float>();
+        if (!im) { delete p; return JT_ENOMEM; }
+        fill(im);
+        p->impl = im;
+    } else {
+        auto *im = new (std::nothrow) PlanImpl<double>();
+        if (!im) { delete p; return JT_ENOMEM; }
+        fill(im);
+        p->impl = im;
+    }
+    // Build the tables the transform's main ops use now, as the reference
+    // constructors do, so execution does no setup work.
+    int st = JT_OK;
+    int main_op = kind == JT_FFT ? JT_COMPLEX_FORWARD : JT_FORWARD;
+    if (prec == JT_FLOAT32) st = impl_of<float>(p)->prepare(main_op);
+    else st = impl_of<double>(p)->prepare(main_op);
+    if (st == JT_OK && cudaDeviceSynchronize() != cudaSuccess) st = JT_ECUDA;
+    if (st != JT_OK) {
+        jt_plan_destroy(p);
+        return st;
+    }
+    *out = p;
+    return JT_OK;
+}
+
+int jt_plan_destroy(jt_plan *p) {
+    if (!p) return JT_EINVAL;
+    cudaDeviceSynchronize();
+    if (p->prec == JT_FLOAT32) delete (PlanImpl<float> *)p->impl;
+    else delete (PlanImpl<double> *)p->impl;
+    delete p;
+    return JT_OK;
+}
+
+int jt_plan_extent(const jt_plan *p, int op, int64_t *out_len) {
+    if (!p || !out_len) return JT_EINVAL;
+    JT_TRY(check_op(p, op));
+    *out_len = p->prec == JT_FLOAT32 ? ((PlanImpl<float> *)p->impl)->extent(op) : ((PlanImpl<double> *)p->impl)->extent(op);
+    return JT_OK;
+}
+
+int jt_plan_set_mode(jt_plan *p, int mode) {
+    if (!p) return JT_EINVAL;
+    if (mode == JT_MODE_FP32) {
+        p->mode = mode;
+        return JT_OK;
+    }
+    return JT_EINVAL;
+}
+
+int jt_plan_algorithm(const jt_plan *p, int axis) {
+    if (!p || axis < 0 || axis >= p->nd) return JT_EINVAL;
+    int64_t n = p->dims[axis];
+    if (n == 1) return ALG_TRIVIAL;
+    if (p->prec == JT_FLOAT32) {
+        if (Fft1<float>::direct_ok(n)) return ALG_DIRECT;
+    } else if (Fft1<double>::direct_ok(n)) {
+        return ALG_DIRECT;
+    }
+    PlanImpl<float> *imf = p->prec == JT_FLOAT32 ? (PlanImpl<float> *)p->impl : nullptr;
+    PlanImpl<double> *imd = p->prec == JT_FLOAT64 ? (PlanImpl<double> *)p->impl : nullptr;
+    if (imf && imf->fft.count(n)) return imf->fft.at(n)->algo;
+    if (imd && imd->fft.count(n)) return imd->fft.at(n)->algo;
+    return JT_EINVAL;
+}
+
+int jt_execute(jt_plan *p, int op, void *host, int64_t len, int64_t off, int scale) {
+    return jt_execute_batch(p, op, host, len, off, 1, 0, scale);
+}
+
+int jt_execute_batch(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t batch, int64_t dist, int scale) {
+    if (!p) return JT_EINVAL;
+    JT_TRY(check_op(p, op));
+    if (p->prec == JT_FLOAT32) return exec_host<float>(p, op, host, len, off, batch, dist, scale);
+    return exec_host<double>(p, op, host, len, off, batch, dist, scale);
+}
+
+int jt_execute_device(jt_plan *p, int op, void *dev, int64_t batch, int64_t dist, int scale, void *stream) {
+    if (!p || !dev || batch < 0) return JT_EINVAL;
+    JT_TRY(check_op(p, op));
+    if (batch == 0) return JT_OK;
+    int64_t ext = 0;
+    JT_TRY(jt_plan_extent(p, op, &ext));
+    if (batch > 1 && dist < ext) return JT_EINVAL;
+    if (batch == 1 && dist < ext) dist = (ext + 1) & ~(int64_t)1;
+    size_t esz = p->prec == JT_FLOAT32 ? 4 : 8;
+    // FFT ops view the array as complex pairs: every array must start on a
+    // pair boundary
+    if (p->kind == JT_FFT && (((uintptr_t)dev % (2 * esz)) != 0 || (batch > 1 && (dist % 2) != 0))) return JT_EINVAL;
+    JT_TRY(device_init());
+    JT_TRY(ensure_stream());
+    cudaStream_t s = stream ? (cudaStream_t)stream : t_state.stream;
+    if (p->prec == JT_FLOAT32) return run_device<float>(p, op, (float *)dev, batch, dist, scale != 0, s);
+    return run_device<double>(p, op, (double *)dev, batch, dist, scale != 0, s);
+}
+
+int jt_synchronize(void) {
+    JT_TRY(ensure_stream());
+    JT_CU(cudaStreamSynchronize(t_state.stream));
+    if (t_state.last && t_state.last != t_state.stream) JT_CU(cudaStreamSynchronize(t_state.last));
+    JT_CU(cudaGetLastError());
+    return JT_OK;
+}
+
+const char *jt_strerror(int s) {
+    switch (s) {
+        case JT_OK: return "ok";
+        case JT_EBADSIZE: return "size must be >= 1 (1D) or > 1 (2D/3D)";
+        case JT_ESHORTBUF: return "array too short for offset and transform extent";
+        case JT_ENOTPOW2: return "rows and columns must be power of two numbers";
+        case JT_ECUDA: return "CUDA error";
+        case JT_ETIMEOUT: return "device wait timed out";
+        case JT_EINVAL: return "invalid argument";
+        case JT_ENOMEM: return "device out of memory";
+        case JT_ENODEV: return "no CUDA device";
+        case JT_ETOOBIG: return "size beyond this build's single-GPU limit";
+    }
+    return "unknown status";
+}
+
+int jt_last_cuda_error(void) { return g_last_cuda; }
+
+int64_t jt_launch_count(int reset) {
+    int64_t v = g_launches;
+    if (reset) g_launches = 0;
+    return v;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Mixed-size batch (config "10,000 mixed 1D transforms")
+// ===========================================================================
+struct jt_batch {
+    std::vector<jt_plan *> plans;
+    std::vector<int> ops, scales;
+    std::vector<void *> ptrs;
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graph_stream = nullptr;
+};
+
+extern "C" {
+
+int jt_batch_create(int count, jt_plan *const *plans, const int *ops, void *const *dev_ptrs, const int *scales, jt_batch **out) {
+    if (!out || count < 0 || (count > 0 && (!plans || !ops || !dev_ptrs || !scales))) return JT_EINVAL;
+    *out = nullptr;
+    jt_batch *b = new (std::nothrow) jt_batch();
+    if (!b) return JT_ENOMEM;
+    for (int i = 0; i < count; i++) {
+        if (!plans[i] || plans[i]->nd != 1 || !dev_ptrs[i]) { delete b; return JT_EINVAL; }
+        int st = check_op(plans[i], ops[i]);
+        if (st != JT_OK) { delete b; return st; }
+        b->plans.push_back(plans[i]);
+        b->ops.push_back(ops[i]);
+        b->ptrs.push_back(dev_ptrs[i]);
+        b->scales.push_back(scales[i]);
+    }
+    *out = b;
+    return JT_OK;
+}
+
+int jt_batch_run_per_transform(jt_batch *b, void *stream) {
+    if (!b) return JT_EINVAL;
+    for (size_t i = 0; i < b->plans.size(); i++) {
+        int64_t ext = 0;
+        JT_TRY(jt_plan_extent(b->plans[i], b->ops[i], &ext));
+        JT_TRY(jt_execute_device(b->plans[i], b->ops[i], b->ptrs[i], 1, (ext + 1) & ~(int64_t)1, b->scales[i], stream));
+    }
+    return JT_OK;
+}
+
+int jt_batch_run(jt_batch *b, void *stream) { return jt_batch_run_per_transform(b, stream); }
+
+int jt_batch_run_graph(jt_batch *b, void *stream) {
+    if (!b) return JT_EINVAL;
+    JT_TRY(device_init());
+    JT_TRY(ensure_stream());
+    cudaStream_t s = stream ? (cudaStream_t)stream : t_state.stream;
+    if (!b->graph || b->graph_stream != s) {
+        // size every plan's tables and the scratch outside the capture
+        JT_TRY(jt_batch_run(b, s));
+        JT_CU(cudaStreamSynchronize(s));
+        t_state.last = s;
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        cudaGraph_t g = nullptr;
+        JT_CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int st = jt_batch_run(b, s);
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (st != JT_OK) { if (g) cudaGraphDestroy(g); return st; }
+        if (e != cudaSuccess) { g_last_cuda = (int)e; return JT_ECUDA; }
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { g_last_cuda = (int)e; return JT_ECUDA; }
+        b->graph_stream = s;
+    }
+    JT_CU(cudaGraphLaunch(b->graph, s));
+    g_launches++;
+    return JT_OK;
+}
+
+int jt_batch_destroy(jt_batch *b) {
+    if (!b) return JT_EINVAL;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    delete b;
+    return JT_OK;
+}
+
+}  // extern "C"
