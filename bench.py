@@ -349,22 +349,25 @@ def run_ours(args, world, rank, local):
         err[f"2^{int(math.log2(n))}"] = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
 
     # end to end through the C ABI with pinned host buffers
-    e2e_steps = max(1, min(args.steps, 3))
-    host = []
-    for i, n in enumerate(SIZES):
-        h = torch.empty(2 * ELEMS, dtype=torch.float32, pin_memory=True)
-        h.copy_(pristine[i])
-        host.append(h.numpy())
+    e2e_val = None
     del work
-    torch.cuda.synchronize()
-    for i, n in enumerate(SIZES):  # warm the host path
-        plans[i].plan.execute(N.COMPLEX_FORWARD, host[i][: 2 * n * 4], 0, False, batch=4, dist=2 * n)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    if not args.no_e2e:
+        e2e_steps = max(1, min(args.steps, 3))
+        host = []
         for i, n in enumerate(SIZES):
-            plans[i].plan.execute(N.COMPLEX_FORWARD, host[i], 0, False, batch=ELEMS // n, dist=2 * n)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_val = flops_step / world / e2e_s / 1e9 * world
+            h = torch.empty(2 * ELEMS, dtype=torch.float32, pin_memory=True)
+            h.copy_(pristine[i])
+            host.append(h.numpy())
+        torch.cuda.synchronize()
+        for i, n in enumerate(SIZES):  # warm the host path
+            plans[i].plan.execute(N.COMPLEX_FORWARD, host[i][: 2 * n * 4], 0, False, batch=4, dist=2 * n)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for i, n in enumerate(SIZES):
+                plans[i].plan.execute(N.COMPLEX_FORWARD, host[i], 0, False, batch=ELEMS // n, dist=2 * n)
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e_val = flops_step / e2e_s / 1e9
+        del host
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -378,7 +381,7 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * ELEMS * len(SIZES),
                     "d2h_bytes_per_step": 8 * ELEMS * len(SIZES),
                     "path": "FloatFFT_1D plan -> jt_execute_batch on pinned host arrays"},
-            "gpu_launches": launches // max(args.steps, 1) * 0 + launches,
+            "gpu_launches": launches,
             "timed_wall_s": wall}
     clocks = clk.summary()
     line["clocks"] = clocks
@@ -408,7 +411,19 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-other", action="store_true", help="skip the other workloads")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: 256 MiB per size instead of 1 GiB, no e2e/CPU/other workloads")
+    ap.add_argument("--sizes", type=str, default="", help="comma-separated subset of the headline sizes")
     args = ap.parse_args()
+    global ELEMS, SIZES
+    if args.small:
+        ELEMS = 2 ** 25
+        args.no_cpu = args.no_other = True
+        args.no_e2e = True
+    else:
+        args.no_e2e = False
+    if args.sizes:
+        SIZES = [int(s) for s in args.sizes.split(",")]
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup(args)
     if args.impl == "reference":

@@ -107,8 +107,8 @@ int jt_execute_batch(jt_plan *plan, int op, void *host_array, int64_t array_len,
                      int64_t offset, int64_t batch, int64_t dist, int scale);
 
 /* `batch` transforms in place on DEVICE memory, transform b at
- * dev_array + b*dist scalars, on `stream` (a cudaStream_t; NULL = the calling
- * thread's stream).  Asynchronous: returns after the launches. */
+ * dev_array + b*dist scalars, on `stream` (a cudaStream_t; NULL = CUDA's
+ * default stream).  Asynchronous: returns after the launches. */
 int jt_execute_device(jt_plan *plan, int op, void *dev_array, int64_t batch,
                       int64_t dist, int scale, void *stream);
 

@@ -462,18 +462,17 @@ __global__ void bluestein_post_kernel(C2 *a, int64_t dist, const C2 *tmp, const 
 // Real FFT pack / unpack (even n, h = n/2 complex points).
 // Wr[k] = e^{-2 pi i k / n}, k <= n/4.
 // ---------------------------------------------------------------------------
-// X_k from Z (the h-point FFT of z_j = x_2j + i x_2j+1), SIGN=-1.
-// For SIGN=+1 (inverse-full) the input is the e^{+} FFT and the conjugate
-// twiddle gives the e^{+} real transform.
-template <int SIGN, typename T>
+// X_k from Z (the h-point FFT of z_j = x_2j + i x_2j+1):
+//   X_k = 0.5 (Z_k + conj Z_{h-k}) - 0.5 i w (Z_k - conj Z_{h-k})
+// with w = e^{-2 pi i k/n} for the forward transform.  The same formula with
+// w = e^{+2 pi i k/n} turns the e^{+} h-point FFT into the e^{+} n-point real
+// transform (realInverseFull); only the twiddle changes.
+template <typename T>
 __device__ __forceinline__ void real_split(C2 zk, C2 zh, C2 w, C2 &xk) {
-    // xk = 0.5 (zk + conj zh) - 0.5 i w (zk - conj zh), w = e^{SIGN 2 pi i k/n}
     C2 a = mk<T>((T)0.5 * (zk.x + zh.x), (T)0.5 * (zk.y - zh.y));
     C2 d = mk<T>((T)0.5 * (zk.x - zh.x), (T)0.5 * (zk.y + zh.y));
     C2 wd = cmul<T>(w, d);
-    // -i * wd = (wd.y, -wd.x) for SIGN -1;  +i * wd for SIGN +1
-    if (SIGN < 0) xk = mk<T>(a.x + wd.y, a.y - wd.x);
-    else xk = mk<T>(a.x - wd.y, a.y + wd.x);
+    xk = mk<T>(a.x + wd.y, a.y - wd.x);  // a - i * wd
 }
 
 // In place: a holds Z (h complex); writes the packed realForward layout.
@@ -493,10 +492,10 @@ __global__ void real_post_packed_kernel(T *a, int64_t dist, int64_t n, int64_t b
     C2 zk = z[k], zh = z[k2];
     C2 w = __ldg(&Wr[k]);
     C2 xk, xh;
-    real_split<-1, T>(zk, zh, w, xk);
+    real_split<T>(zk, zh, w, xk);
     if (k2 != k) {
         // w_{h-k} = -conj(w_k)
-        real_split<-1, T>(zh, zk, mk<T>(-w.x, w.y), xh);
+        real_split<T>(zh, zk, mk<T>(-w.x, w.y), xh);
         z[k2] = xh;
     }
     z[k] = xk;
@@ -525,12 +524,12 @@ __global__ void real_post_full_kernel(const T *zin, int64_t zdist, T *out, int64
     C2 w = __ldg(&Wr[k]);
     if (SIGN > 0) w.y = -w.y;
     C2 xk, xh;
-    real_split<SIGN, T>(zk, zh, w, xk);
+    real_split<T>(zk, zh, w, xk);
     xk = cscale<T>(xk, s);
     F[k] = xk;
     F[n - k] = cconj<T>(xk);
     if (k2 != k) {
-        real_split<SIGN, T>(zh, zk, mk<T>(-w.x, w.y), xh);
+        real_split<T>(zh, zk, mk<T>(-w.x, w.y), xh);
         xh = cscale<T>(xh, s);
         F[k2] = xh;
         F[n - k2] = cconj<T>(xh);

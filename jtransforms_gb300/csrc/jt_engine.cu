@@ -13,6 +13,7 @@
 //             nextPow2(2n-1) points (fft/DoubleFFT_1D.java:1864-2107), chirp
 //             tables generated in FP64 on the device.
 #include "jt_device.cuh"
+#include "jt_stockham.cuh"
 #include "../../include/jtgpu.h"
 
 #include <algorithm>
@@ -109,6 +110,12 @@ static int device_init() {
     return g_dev_status;
 }
 
+// Register-resident power-of-two kernel launchers (jt_pow2_f32.cu, jt_pow2_f64.cu).
+bool stockham_launch(int L, int mode, int sign, const float2 *in, float2 *out, const StockParams &p, const float2 *W,
+                     const float2 *Whi, const float2 *Wlo, cudaStream_t s);
+bool stockham_launch(int L, int mode, int sign, const double2 *in, double2 *out, const StockParams &p, const double2 *W,
+                     const double2 *Whi, const double2 *Wlo, cudaStream_t s);
+
 // ---------------------------------------------------------------------------
 // Complex FFT of one length
 // ---------------------------------------------------------------------------
@@ -157,7 +164,15 @@ template <typename T> struct Fft1 {
             if (p) cudaFree(p);
     }
 
-    static bool direct_ok(int64_t n) { return n >= 2 && n <= Lim<T>::lmax() && !direct_radices(n).empty(); }
+    static bool generic_ok(int64_t n) { return n >= 2 && n <= Lim<T>::lmax() && !direct_radices(n).empty(); }
+    // register-resident power-of-two kernel (jt_stockham.cuh): row mode up to
+    // reg_rows_max, column modes up to 4096
+    static int64_t reg_rows_max() { return sizeof(T) == 4 ? 16384 : 8192; }
+    static bool reg_ok(int64_t n) { return is_pow2(n) && n >= 16 && n <= reg_rows_max(); }
+    static bool direct_ok(int64_t n) { return reg_ok(n) || generic_ok(n); }
+    bool reg = false;
+    // whether a line pass with strided (column) layouts can run in one kernel
+    bool cols_ok() const { return algo == ALG_DIRECT && (reg ? n <= 4096 : true); }
 
     static int make_roots(C2 **out, int64_t count, int64_t num, int64_t den) {
         JT_CU(cudaMalloc(out, sizeof(C2) * std::max<int64_t>(count, 1)));
@@ -175,17 +190,22 @@ template <typename T> struct Fft1 {
             f->algo = ALG_TRIVIAL;
         } else if (direct_ok(n)) {
             f->algo = ALG_DIRECT;
-            f->radix = direct_radices(n);
+            f->reg = reg_ok(n);
+            if (!f->reg) f->radix = direct_radices(n);
             JT_TRY(make_roots(&f->W, n, 1, n));
         } else {
-            // balanced split into two DIRECT lengths
+            // two DIRECT lengths, n = n1 (column pass) * n2 (row pass): as
+            // balanced as possible, preferring lengths both passes run on
+            // the register kernel (n1, n2 <= 4096 powers of two)
             int64_t best = 0;
             double bestd = 1e300;
-            for (int64_t d = 2; d <= Lim<T>::lmax() && d < n; d++) {
+            for (int64_t d = 2; d <= reg_rows_max() && d < n; d++) {
                 if (n % d) continue;
                 int64_t e = n / d;
                 if (!direct_ok(d) || !direct_ok(e)) continue;
-                double dd = std::fabs(std::log((double)d) - std::log((double)e));
+                bool fast = reg_ok(d) && reg_ok(e) && d <= 4096 && e <= 4096;
+                if (!fast && (!generic_ok(d) || !generic_ok(e))) continue;
+                double dd = std::fabs(std::log((double)d) - std::log((double)e)) - (fast ? 100.0 : 0.0);
                 if (dd < bestd) { bestd = dd; best = d; }
             }
             if (best) {
@@ -194,6 +214,13 @@ template <typename T> struct Fft1 {
                 f->n2 = n / best;
                 JT_TRY(create(f->n1, f->pa));
                 JT_TRY(create(f->n2, f->pb));
+                // pass A reads and writes columns, pass B writes columns: the
+                // register kernel does that up to 4096, the generic one always
+                for (Fft1 *sub : {f->pa.get(), f->pb.get()})
+                    if (sub->reg && sub->n > 4096) {
+                        sub->reg = false;
+                        sub->radix = direct_radices(sub->n);
+                    }
                 f->lo_bits = 0;
                 while (((int64_t)1 << (2 * f->lo_bits)) < n) f->lo_bits++;
                 int64_t nlo = (int64_t)1 << f->lo_bits;
@@ -218,6 +245,26 @@ template <typename T> struct Fft1 {
                     double scale, int64_t tw_n = 0, int64_t tw_inner = 1, const C2 *Whi_ = nullptr, const C2 *Wlo_ = nullptr,
                     int tw_lo_bits = 0) const {
         if (nlines <= 0) return JT_OK;
+        if (reg) {
+            int mode = -1;
+            if (lin.estride == 1 && lout.estride == 1) mode = 0;
+            else if (lin.estride != 1 && lout.estride != 1 && n <= 4096) mode = 1;
+            else if (lin.estride == 1 && lout.estride != 1 && n <= 4096) mode = 2;
+            if (mode < 0) return JT_EINVAL;
+            StockParams sp;
+            memset(&sp, 0, sizeof(sp));
+            sp.nlines = nlines;
+            sp.lin = lin;
+            sp.lout = lout;
+            sp.scale = scale;
+            sp.tw_n = tw_n;
+            sp.tw_inner = tw_inner;
+            sp.tw_lo_bits = tw_lo_bits;
+            if (ctx.dry) return JT_OK;
+            if (!stockham_launch((int)n, mode, sign, in, out, sp, W, Whi_, Wlo_, ctx.s)) return JT_EINVAL;
+            g_launches++;
+            return JT_OK;
+        }
         const int L = (int)n;
         const int Lp = padded_len(L);
         const bool strided = lin.estride != 1 || lout.estride != 1;
@@ -623,7 +670,7 @@ template <typename T> struct PlanImpl {
             double s = (sign > 0 && scale) ? 1.0 / (double)len : 1.0;
             if (inner == 1) {
                 JT_TRY(f->exec(ctx, a, len, a, len, outer, sign, s));
-            } else if (f->algo == ALG_DIRECT) {
+            } else if (f->cols_ok()) {
                 Layout l = {inner, len * inner, 1, inner};
                 JT_TRY(f->exec_direct(ctx, a, a, outer * inner, l, l, sign, s));
             } else if (f->algo == ALG_TRIVIAL) {
@@ -753,7 +800,7 @@ template <typename T> struct PlanImpl {
 
     // Column pass over `cols` complex columns of `rows` rows, batch arrays.
     int column_fft(Ctx &ctx, Fft1<T> *f, C2 *a, int64_t batch, int64_t rows, int64_t cols, const Layout &l, int sign, double s) {
-        if (f->algo == ALG_DIRECT) return f->exec_direct(ctx, a, a, batch * cols, l, l, sign, s);
+        if (f->cols_ok()) return f->exec_direct(ctx, a, a, batch * cols, l, l, sign, s);
         if (f->algo == ALG_TRIVIAL) return JT_OK;
         C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * rows * cols, ctx.dry);
         transpose<C2>(ctx, a, tmp, batch, rows, cols);
@@ -1034,7 +1081,7 @@ int jt_execute_device(jt_plan *p, int op, void *dev, int64_t batch, int64_t dist
     if (p->kind == JT_FFT && (((uintptr_t)dev % (2 * esz)) != 0 || (batch > 1 && (dist % 2) != 0))) return JT_EINVAL;
     JT_TRY(device_init());
     JT_TRY(ensure_stream());
-    cudaStream_t s = stream ? (cudaStream_t)stream : t_state.stream;
+    cudaStream_t s = (cudaStream_t)stream;
     if (p->prec == JT_FLOAT32) return run_device<float>(p, op, (float *)dev, batch, dist, scale != 0, s);
     return run_device<double>(p, op, (double *)dev, batch, dist, scale != 0, s);
 }
