@@ -214,7 +214,9 @@ struct TileParams {
     int C;            // lines per tile
     int64_t nlines;
     Layout lin, lout;
-    double scale;     // output multiplier (1 = none)
+    double scale;     // output multiplier (1 = none), double plans
+    float scalef;     // the same for float plans (no FP64 work in float kernels)
+    int do_scale;
     int64_t tw_n;     // four-step post twiddle w_{tw_n}^{sign*k*(b % tw_inner)}; 0 = none
     int64_t tw_inner;
     int tw_lo_bits;
@@ -352,8 +354,10 @@ __global__ void __launch_bounds__(512) fft_tile_kernel(const C2 *in, C2 *out, Ti
         Ns *= R;
     }
 
-    const T sc = (T)p.scale;
-    const bool do_scale = p.scale != 1.0;
+    T sc;
+    if constexpr (sizeof(T) == 4) sc = p.scalef;
+    else sc = (T)p.scale;
+    const bool do_scale = p.do_scale != 0;
     const int64_t lo_mask = ((int64_t)1 << p.tw_lo_bits) - 1;
     if (p.lout.estride == 1) {
         for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
@@ -448,13 +452,13 @@ __global__ void bluestein_mul_kernel(C2 *tmp, const C2 *__restrict__ bk2, int64_
 
 template <int SIGN, typename T>
 __global__ void bluestein_post_kernel(C2 *a, int64_t dist, const C2 *tmp, const C2 *__restrict__ bk1, int64_t n, int64_t nB,
-                                      int64_t batch, double scale) {
+                                      int64_t batch, T scale) {
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
     C2 x = tmp[b * nB + i], w = __ldg(&bk1[i]);
     C2 v = SIGN < 0 ? cmulc<T>(x, w) : cmul<T>(x, w);
-    if (scale != 1.0) v = cscale<T>(v, (T)scale);
+    if (scale != (T)1) v = cscale<T>(v, scale);
     a[b * dist + i] = v;
 }
 
@@ -505,14 +509,14 @@ __global__ void real_post_packed_kernel(T *a, int64_t dist, int64_t n, int64_t b
 // SIGN=+1 writes the e^{+} transform (z must be the e^{+} FFT), times scale.
 template <int SIGN, typename T>
 __global__ void real_post_full_kernel(const T *zin, int64_t zdist, T *out, int64_t odist, int64_t n, int64_t batch,
-                                      const C2 *__restrict__ Wr, double scale) {
+                                      const C2 *__restrict__ Wr, T scale) {
     const int64_t h = n / 2, q = h / 2 + 1;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * q) return;
     int64_t b = idx / q, k = idx - b * q;
     const C2 *z = reinterpret_cast<const C2 *>(zin + b * zdist);
     C2 *F = reinterpret_cast<C2 *>(out + b * odist);
-    const T s = (T)scale;
+    const T s = scale;
     if (k == 0) {
         C2 z0 = z[0];
         F[0] = mk<T>((z0.x + z0.y) * s, 0);
@@ -539,13 +543,13 @@ __global__ void real_post_full_kernel(const T *zin, int64_t zdist, T *out, int64
 // In place: packed spectrum -> Z (h complex) whose e^{+} h-point FFT is
 // (n/2) * x interleaved; everything times `mult`.
 template <typename T>
-__global__ void real_pre_inverse_kernel(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr, double mult) {
+__global__ void real_pre_inverse_kernel(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr, T mult) {
     const int64_t h = n / 2, q = h / 2 + 1;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * q) return;
     int64_t b = idx / q, k = idx - b * q;
     C2 *z = reinterpret_cast<C2 *>(a + b * dist);
-    const T m = (T)mult;
+    const T m = mult;
     if (k == 0) {
         C2 x = z[0];  // (X0, X_{n/2})
         z[0] = mk<T>((T)0.5 * (x.x + x.y) * m, (T)0.5 * (x.x - x.y) * m);
@@ -617,23 +621,23 @@ __global__ void unpack_to_full_kernel(const T *a, int64_t dist, C2 *F, int64_t n
 
 // a[b][i] = Re(F[b][i]) * mult
 template <typename T>
-__global__ void real_part_kernel(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch, double mult) {
+__global__ void real_part_kernel(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch, T mult) {
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
-    a[b * dist + i] = F[idx].x * (T)mult;
+    a[b * dist + i] = F[idx].x * mult;
 }
 
 // Copies batch*len complex (strided) with an optional scale and conjugation.
 template <typename T>
 __global__ void copy_complex_kernel(const C2 *src, int64_t sdist, C2 *dst, int64_t ddist, int64_t len, int64_t batch,
-                                    double scale, int conj) {
+                                    T scale, int conj) {
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * len) return;
     int64_t b = idx / len, i = idx - b * len;
     C2 v = src[b * sdist + i];
     if (conj) v.y = -v.y;
-    if (scale != 1.0) v = cscale<T>(v, (T)scale);
+    if (scale != (T)1) v = cscale<T>(v, scale);
     dst[b * ddist + i] = v;
 }
 
@@ -668,13 +672,13 @@ template <typename T> __device__ __forceinline__ C2 packed_get(const T *p, int64
 // C_k = Re(e^{-i pi k/2n} V_k) * mult (k=0: * mult0); DST writes C_k to n-1-k.
 template <typename T>
 __global__ void dct2_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch,
-                                 const C2 *__restrict__ Wd, double mult, double mult0, int dst) {
+                                 const C2 *__restrict__ Wd, T mult, T mult0, int dst) {
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * n) return;
     int64_t b = idx / n, k = idx - b * n;
     C2 V = packed_get<T>(v + b * vdist, n, k);
     C2 w = __ldg(&Wd[k]);
-    T c = (w.x * V.x - w.y * V.y) * (T)(k == 0 ? mult0 : mult);
+    T c = (w.x * V.x - w.y * V.y) * (k == 0 ? mult0 : mult);
     a[b * dist + (dst ? n - 1 - k : k)] = c;
 }
 
@@ -683,7 +687,7 @@ __global__ void dct2_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, 
 // g_0 = mult0, g_k = mult.  Thread k <= n/2 writes V_k.
 template <typename T>
 __global__ void dct3_pre_kernel(const T *a, int64_t dist, T *v, int64_t vdist, int64_t n, int64_t batch,
-                                const C2 *__restrict__ Wd, double mult, double mult0, int dst) {
+                                const C2 *__restrict__ Wd, T mult, T mult0, int dst) {
     const int64_t q = n / 2 + 1;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * q) return;
@@ -719,12 +723,12 @@ __global__ void dct3_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, 
 
 // H_k = Re X_k - Im X_k from the packed spectrum (dht/DoubleDHT_1D.java:94-159)
 template <typename T>
-__global__ void dht_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, double mult) {
+__global__ void dht_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, T mult) {
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * n) return;
     int64_t b = idx / n, k = idx - b * n;
     C2 X = packed_get<T>(v + b * vdist, n, k);
-    a[b * dist + k] = (X.x - X.y) * (T)mult;
+    a[b * dist + k] = (X.x - X.y) * mult;
 }
 
 // ---------------------------------------------------------------------------
@@ -829,7 +833,7 @@ __global__ void transpose_kernel(const E *in, E *out, int64_t R, int64_t C, int6
     }
 }
 
-template <typename T> __global__ void scale_kernel(T *a, int64_t dist, int64_t len, int64_t batch, double s) {
+template <typename T> __global__ void scale_kernel(T *a, int64_t dist, int64_t len, int64_t batch, T s) {
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * len) return;
     int64_t b = idx / len, i = idx - b * len;

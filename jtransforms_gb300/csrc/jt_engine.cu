@@ -16,6 +16,8 @@
 #include "jt_stockham.cuh"
 #include "../../include/jtgpu.h"
 
+#include <cuda.h>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -88,6 +90,12 @@ static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
     } while (0)
 
 static int g_smem_optin = 0;
+static int g_sms = 1;
+static int *g_err_dev = nullptr;  // raised by a kernel whose bounded wait gave up
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *, const cuuint64_t *,
+                                  const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn g_encode_tiled = nullptr;
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
 
@@ -101,6 +109,16 @@ static int device_init() {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaMalloc(&g_err_dev, sizeof(int)) != cudaSuccess || cudaMemset(g_err_dev, 0, sizeof(int)) != cudaSuccess) {
+            g_dev_status = JT_ECUDA;
+            return;
+        }
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode_tiled = (EncodeTiledFn)fn;
         cudaFuncSetAttribute(fft_tile_kernel<-1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(fft_tile_kernel<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(fft_tile_kernel<-1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
@@ -111,10 +129,30 @@ static int device_init() {
 }
 
 // Register-resident power-of-two kernel launchers (jt_pow2_f32.cu, jt_pow2_f64.cu).
-bool stockham_launch(int L, int mode, int sign, const float2 *in, float2 *out, const StockParams &p, const float2 *W,
-                     const float2 *Whi, const float2 *Wlo, cudaStream_t s);
-bool stockham_launch(int L, int mode, int sign, const double2 *in, double2 *out, const StockParams &p, const double2 *W,
-                     const double2 *Whi, const double2 *Wlo, cudaStream_t s);
+bool stockham_launch(int L, int mode, int sign, const float2 *in, float2 *out, const StockParams &p, const CUtensorMap *tmap,
+                     const float2 *W, const float2 *Whi, const float2 *Wlo, int *err, int sms, cudaStream_t s);
+bool stockham_launch(int L, int mode, int sign, const double2 *in, double2 *out, const StockParams &p, const CUtensorMap *tmap,
+                     const double2 *W, const double2 *Whi, const double2 *Wlo, int *err, int sms, cudaStream_t s);
+bool stockham_pipe_ok(int L, int mode, const float *);
+bool stockham_pipe_ok(int L, int mode, const double *);
+int stockham_lines_per_cta(int L, int mode, const float *);
+int stockham_lines_per_cta(int L, int mode, const double *);
+
+// Encodes a 3D tiled tensor map over complex elements of esz bytes (8 or 16,
+// moved as 8-byte units): x = column (inner), y = row, z = outer block.
+static bool make_col_tmap(CUtensorMap *m, const void *base, int esz, int64_t inner, int64_t rows, int64_t nblocks,
+                          int64_t row_pitch, int64_t block_stride, int C, int BR) {
+    if (!g_encode_tiled) return false;
+    const int xm = esz / 8;
+    cuuint64_t dims[3] = {(cuuint64_t)(inner * xm), (cuuint64_t)rows, (cuuint64_t)nblocks};
+    cuuint64_t strides[2] = {(cuuint64_t)(row_pitch * esz), (cuuint64_t)(block_stride * esz)};
+    cuuint32_t box[3] = {(cuuint32_t)(C * xm), (cuuint32_t)BR, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    if ((row_pitch * esz) % 16 || (block_stride * esz) % 16 || ((uintptr_t)base % 16)) return false;
+    return g_encode_tiled(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(base), dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 // ---------------------------------------------------------------------------
 // Complex FFT of one length
@@ -257,11 +295,31 @@ template <typename T> struct Fft1 {
             sp.lin = lin;
             sp.lout = lout;
             sp.scale = scale;
+            sp.scalef = (float)scale;
+            sp.do_scale = scale != 1.0;
             sp.tw_n = tw_n;
             sp.tw_inner = tw_inner;
             sp.tw_lo_bits = tw_lo_bits;
             if (ctx.dry) return JT_OK;
-            if (!stockham_launch((int)n, mode, sign, in, out, sp, W, Whi_, Wlo_, ctx.s)) return JT_EINVAL;
+            // TMA pipeline when the 16-byte rules hold, else the plain kernel
+            const int esz = (int)sizeof(C2);
+            const int Cl = stockham_lines_per_cta((int)n, mode, (const T *)nullptr);
+            CUtensorMap tm;
+            memset(&tm, 0, sizeof(tm));
+            bool pipe = stockham_pipe_ok((int)n, mode, (const T *)nullptr) && ((uintptr_t)in % 16) == 0;
+            if (pipe && mode == 1) {
+                pipe = lin.istride == 1 && lin.inner % Cl == 0 && nlines % lin.inner == 0 &&
+                       make_col_tmap(&tm, in, esz, lin.inner, n, nlines / lin.inner, lin.estride, lin.outer, Cl,
+                                     (int)std::min<int64_t>(n, 256));
+                sp.tiles_per_col = lin.inner / Cl;
+            } else if (pipe) {
+                bool contig = lin.inner == 1 && lin.outer == n;
+                pipe = contig || ((lin.outer * esz) % 16 == 0 && (lin.inner == 1 || (lin.istride * esz) % 16 == 0));
+                pipe = pipe && (n * esz) % 16 == 0;
+            }
+            if (!stockham_launch((int)n, mode, sign, in, out, sp, pipe ? &tm : nullptr, W, Whi_, Wlo_, g_err_dev, g_sms,
+                                 ctx.s))
+                return JT_EINVAL;
             g_launches++;
             return JT_OK;
         }
@@ -287,6 +345,8 @@ template <typename T> struct Fft1 {
         p.lin = lin;
         p.lout = lout;
         p.scale = scale;
+        p.scalef = (float)scale;
+        p.do_scale = scale != 1.0;
         p.tw_n = tw_n;
         p.tw_inner = tw_inner;
         p.tw_lo_bits = tw_lo_bits;
@@ -863,6 +923,17 @@ int ensure_arena(size_t bytes) {
 
 template <typename T> PlanImpl<T> *impl_of(jt_plan *p) { return (PlanImpl<T> *)p->impl; }
 
+// After a synchronize: JT_ETIMEOUT if a kernel's bounded wait gave up.
+int check_err_flag() {
+    int h = 0;
+    JT_CU(cudaMemcpy(&h, g_err_dev, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        JT_CU(cudaMemset(g_err_dev, 0, sizeof(int)));
+        return JT_ETIMEOUT;
+    }
+    return JT_OK;
+}
+
 // Runs op on device memory: dry run to size the scratch, then the launches.
 template <typename T>
 int run_device(jt_plan *p, int op, T *a, int64_t batch, int64_t dist, bool scale, cudaStream_t s) {
@@ -958,7 +1029,7 @@ int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t 
     t_state.last = s;
     JT_CU(cudaStreamSynchronize(s));
     JT_CU(cudaGetLastError());
-    return JT_OK;
+    return check_err_flag();
 }
 
 }  // namespace
@@ -1090,8 +1161,9 @@ int jt_synchronize(void) {
     JT_TRY(ensure_stream());
     JT_CU(cudaStreamSynchronize(t_state.stream));
     if (t_state.last && t_state.last != t_state.stream) JT_CU(cudaStreamSynchronize(t_state.last));
+    JT_CU(cudaDeviceSynchronize());
     JT_CU(cudaGetLastError());
-    return JT_OK;
+    return check_err_flag();
 }
 
 const char *jt_strerror(int s) {

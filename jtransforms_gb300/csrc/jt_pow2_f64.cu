@@ -1,16 +1,36 @@
 // jt_pow2_f64.cu -- instantiations of the register-resident power-of-two
-// Stockham kernel (jt_stockham.cuh) for double.
+// Stockham kernels (jt_stockham.cuh) for double.
 #include "jt_stockham.cuh"
 
 namespace jt {
 
+// Whether the pipelined (TMA) kernel exists for (L, mode).
+bool stockham_pipe_ok(int L, int mode, const double *) {
+#define JT_PCASE(LL) \
+    case LL:         \
+        return mode == 0 ? Stockham<double, LL, 0, -1>::PIPE_OK : (LL <= 4096 && Stockham<double, (LL <= 4096 ? LL : 16), 1, -1>::PIPE_OK);
+    switch (L) {
+        JT_PCASE(16) JT_PCASE(32) JT_PCASE(64) JT_PCASE(128) JT_PCASE(256) JT_PCASE(512) JT_PCASE(1024)
+        JT_PCASE(2048) JT_PCASE(4096) JT_PCASE(8192)
+
+        default: return false;
+    }
+#undef JT_PCASE
+}
+
+// Lines per CTA of (L, mode).
+int stockham_lines_per_cta(int L, int mode, const double *) { return StockCfg<double>::C(L, mode); }
+
 // Launches the kernel for line length L; returns false when (L, mode) has no
-// instantiation (row mode: 16..8192, column modes: 16..4096).
+// instantiation (row mode: 16..8192, column modes: 16..4096).  A non-null
+// `tmap` selects the pipelined TMA kernel (the caller has checked
+// stockham_pipe_ok and the 16-byte rules).
 bool stockham_launch(int L, int mode, int sign, const V2<double>::t *in, V2<double>::t *out, const StockParams &p,
-                     const V2<double>::t *W, const V2<double>::t *Whi, const V2<double>::t *Wlo, cudaStream_t s) {
-#define JT_CASE(LL)                                                         \
-    case LL:                                                                \
-        StockLaunch<double, LL>::go(mode, sign, in, out, p, W, Whi, Wlo, s);  \
+                     const CUtensorMap *tmap, const V2<double>::t *W, const V2<double>::t *Whi, const V2<double>::t *Wlo,
+                     int *err, int sms, cudaStream_t s) {
+#define JT_CASE(LL)                                                                       \
+    case LL:                                                                              \
+        StockLaunch<double, LL>::go(mode, sign, in, out, p, tmap, W, Whi, Wlo, err, sms, s); \
         return true;
     if (mode == 0) {
         switch (L) {
@@ -27,7 +47,5 @@ bool stockham_launch(int L, int mode, int sign, const V2<double>::t *in, V2<doub
     }
 #undef JT_CASE
 }
-
-int stockham_lines_per_cta(int L, int mode, const double *) { return StockCfg<double>::C(L, mode); }
 
 }  // namespace jt

@@ -4,17 +4,27 @@
 // E = 16 elements of one line (t, t+TL, ..., t+15*TL with TL = L/16): the
 // radix-16 butterflies of a pass run in registers and shared memory is used
 // only to exchange data between passes (self-sorting Stockham order, so the
-// result comes out in natural order with no bit reversal).  The first pass
-// reads global memory directly and the last pass writes it directly, both
-// coalesced:
-//   MODE 0  rows in, rows out        (contiguous lines; threads walk a line)
-//   MODE 1  columns in, columns out  (lines C adjacent columns; threads walk
-//           across the columns), optional four-step twiddle on the output
+// result comes out in natural order with no bit reversal).  Three layouts:
+//   MODE 0  rows in, rows out        (contiguous lines)
+//   MODE 1  columns in, columns out  (C adjacent columns per tile), optional
+//           four-step twiddle fused into the store
 //   MODE 2  rows in, columns out     (the transposing row pass of the
-//           four-step scheme: rows are staged through shared memory)
+//           four-step scheme; the store is staged through shared memory)
+//
+// stockham_pipe_kernel is the main kernel: persistent CTAs walk their tiles
+// and the next tile is already in flight while the current one is computed.
+// TMA brings it into a second shared-memory stage: one cp.async.bulk per
+// contiguous run of rows (MODE 0/2) or cp.async.bulk.tensor boxes of
+// C columns x up to 256 rows (MODE 1), completing on an mbarrier.  Every
+// mbarrier wait is bounded; on timeout the kernel raises the error flag,
+// drains its copies (bounded) and returns.  The passes exchange through the
+// stage buffer itself with an XOR swizzle.
+// stockham_kernel is the plain (non-TMA) variant for arrays whose addresses
+// or strides do not meet TMA's 16-byte rules.
 #pragma once
 
 #include "jt_device.cuh"
+#include "jt_tma.cuh"
 
 namespace jt {
 
@@ -24,10 +34,18 @@ __host__ __device__ constexpr int ipowc(int b, int e) { return e == 0 ? 1 : b * 
 struct StockParams {
     int64_t nlines;
     Layout lin, lout;
-    double scale;
+    double scale;  // output multiplier (double plans)
+    float scalef;  // the same for float plans: float kernels do no FP64 work
+    int do_scale;
     int64_t tw_n, tw_inner;  // four-step output twiddle w_{tw_n}^{pos * (b % tw_inner)}; tw_n = 0: none
     int tw_lo_bits;
+    int64_t tiles_per_col;   // MODE 1 pipe: column tiles per outer block (inner / C)
 };
+
+template <typename T> __device__ __forceinline__ T param_scale(const StockParams &p) {
+    if constexpr (sizeof(T) == 4) return p.scalef;
+    else return (T)p.scale;
+}
 
 template <typename T> struct StockCfg {
     // lines per CTA for the row mode: about 256 threads
@@ -60,6 +78,13 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     static constexpr int REM = 1 << (LOGL % LOGE);
     static constexpr int NPASS = NFULL + (REM > 1 ? 1 : 0);
     static constexpr size_t SMEM = (size_t)C * LP * sizeof(C2);
+    // pipelined kernel: two dense stages of C lines and two mbarriers
+    static constexpr int STAGE = C * L;
+    static constexpr size_t PIPE_SMEM = 2 * (size_t)STAGE * sizeof(C2) + 16;
+    static constexpr bool PIPE_OK = PIPE_SMEM <= 227 * 1024;
+    // XOR swizzle of the exchange: G elements per 128-byte row
+    static constexpr int G = 128 / (int)sizeof(C2);
+    static constexpr int LG = ilog2c(G);
 
     template <int P> struct Pass {
         static constexpr int R = P < NFULL ? E : REM;
@@ -70,9 +95,10 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     };
 
     // Butterflies of pass P on the thread's registers; non-last passes write
-    // their outputs to the line's shared-memory row.
-    template <int P, typename Store>
-    static __device__ __forceinline__ void run(C2 (&v)[E], int t, C2 *sl, const C2 *__restrict__ W, Store &store) {
+    // their outputs to shared memory at xs[xi(index)] and read the next
+    // pass's inputs back.
+    template <int P, typename Store, typename XIdx>
+    static __device__ __forceinline__ void run(C2 (&v)[E], int t, C2 *xs, XIdx &xi, const C2 *__restrict__ W, Store &store) {
         typedef Pass<P> PP;
 #pragma unroll
         for (int q = 0; q < PP::NB; q++) {
@@ -93,19 +119,22 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
 #pragma unroll
             for (int k = 0; k < PP::R; k++) {
                 if (PP::LAST) store(idxD + k * PP::NS, u[k]);
-                else sl[pad(idxD + k * PP::NS)] = u[k];
+                else xs[xi(idxD + k * PP::NS)] = u[k];
             }
         }
         if constexpr (!PP::LAST) {
             __syncthreads();
 #pragma unroll
-            for (int m = 0; m < E; m++) v[m] = sl[pad(t + m * TL)];
+            for (int m = 0; m < E; m++) v[m] = xs[xi(t + m * TL)];
             __syncthreads();
-            run<P + 1>(v, t, sl, W, store);
+            run<P + 1>(v, t, xs, xi, W, store);
         }
     }
 };
 
+// ---------------------------------------------------------------------------
+// Plain kernel (no TMA): one tile per CTA.
+// ---------------------------------------------------------------------------
 template <typename T, int L, int MODE, int SIGN>
 __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
     stockham_kernel(const typename V2<T>::t *__restrict__ in, typename V2<T>::t *__restrict__ out, StockParams p,
@@ -127,11 +156,9 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
     const int64_t b0 = (int64_t)blockIdx.x * S::C;
     const int64_t b = b0 + c;
     const bool valid = b < p.nlines;
-    C2 *sl = sm + c * S::LP;
     C2 v[S::E];
 
     if (MODE == 2) {
-        // stage the C rows through shared memory with row-contiguous reads
 #pragma unroll 4
         for (int i = tid; i < S::C * L; i += S::NT) {
             int cc = i >> S::LOGL, e = i & (L - 1);
@@ -139,7 +166,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
         }
         __syncthreads();
 #pragma unroll
-        for (int m = 0; m < S::E; m++) v[m] = sl[pad(t + m * S::TL)];
+        for (int m = 0; m < S::E; m++) v[m] = sm[c * S::LP + pad(t + m * S::TL)];
         __syncthreads();
     } else if (valid) {
         const C2 *src = in + line_off(p.lin, b);
@@ -156,8 +183,8 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
     const bool tw = p.tw_n != 0;
     const int64_t j2 = tw ? b % p.tw_inner : 0;
     const int64_t lo_mask = ((int64_t)1 << p.tw_lo_bits) - 1;
-    const T sc = (T)p.scale;
-    const bool do_scale = p.scale != 1.0;
+    const T sc = param_scale<T>(p);
+    const bool do_scale = p.do_scale != 0;
     auto store = [&](int pos, C2 val) {
         if (tw) {
             int64_t tt = (int64_t)pos * j2;
@@ -167,35 +194,193 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
         if (do_scale) val = cscale<T>(val, sc);
         if (valid) dst[(int64_t)pos * oes] = val;
     };
-    S::template run<0>(v, t, sl, W, store);
+    auto xi = [&](int i) { return c * S::LP + pad(i); };
+    S::template run<0>(v, t, sm, xi, W, store);
 }
 
-// Host-side launcher for one (T, L): picks the instantiation by mode/sign.
+// ---------------------------------------------------------------------------
+// Pipelined persistent kernel (TMA prefetch of the next tile).
+// ---------------------------------------------------------------------------
+#define JT_MBAR_POLL_LIMIT (1u << 22)
+
+template <typename T, int L, int MODE, int SIGN>
+__global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
+    stockham_pipe_kernel(const typename V2<T>::t *__restrict__ in, typename V2<T>::t *__restrict__ out, StockParams p,
+                         const __grid_constant__ CUtensorMap tmap, const typename V2<T>::t *__restrict__ W,
+                         const typename V2<T>::t *__restrict__ Whi, const typename V2<T>::t *__restrict__ Wlo, int *err) {
+    typedef Stockham<T, L, MODE, SIGN> S;
+    typedef typename V2<T>::t C2;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    C2 *stage0 = reinterpret_cast<C2 *>(smem_raw);
+    C2 *stage1 = stage0 + S::STAGE;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(stage1 + S::STAGE);
+    const int tid = threadIdx.x;
+    // MODE 1 walks across columns (c fastest); MODE 0/2 walk along rows
+    int c, t;
+    if (MODE == 1) {
+        c = tid % S::C;
+        t = tid / S::C;
+    } else {
+        c = tid / S::TL;
+        t = tid % S::TL;
+    }
+    const int64_t ntiles = (p.nlines + S::C - 1) / S::C;
+    constexpr uint32_t ESZ = sizeof(C2);
+
+    // Issues the copies of tile `tl` into `st`, completing on `mb`.
+    auto issue = [&](int64_t tl, C2 *st, uint64_t *mb) {
+        const int64_t b0 = tl * S::C;
+        const int lines = (int)min((int64_t)S::C, p.nlines - b0);
+        if (MODE == 1) {
+            // tile = C adjacent columns of one outer block
+            const int64_t ob = tl / p.tiles_per_col;
+            const int col0 = (int)((tl - ob * p.tiles_per_col) * S::C);
+            constexpr int BR = L < 256 ? L : 256;
+            constexpr int XM = sizeof(T) == 4 ? 1 : 2;  // f64 complex = two FLOAT64 in the map
+            mbar_arrive_expect_tx(mb, (uint32_t)(S::STAGE * ESZ));
+#pragma unroll 1
+            for (int r = 0; r < L; r += BR) tensor3d_g2s(st + r * S::C, &tmap, col0 * XM, r, (int)ob, mb);
+        } else if (p.lin.inner == 1 && p.lin.outer == L) {
+            // C consecutive contiguous rows: one copy
+            mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
+            bulk_g2s(st, in + b0 * L, (uint32_t)(lines * L * ESZ), mb);
+        } else {
+            mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
+#pragma unroll 1
+            for (int cc = 0; cc < lines; cc++) bulk_g2s(st + cc * L, in + line_off(p.lin, b0 + cc), (uint32_t)(L * ESZ), mb);
+        }
+    };
+
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        if (MODE == 1) prefetch_tensormap(&tmap);
+    }
+    __syncthreads();
+    int64_t tile = blockIdx.x;
+    if (tid == 0 && tile < ntiles) issue(tile, stage0, &bar[0]);
+
+    const bool tw = p.tw_n != 0;
+    const int64_t lo_mask = ((int64_t)1 << p.tw_lo_bits) - 1;
+    const T sc = param_scale<T>(p);
+    const bool do_scale = p.do_scale != 0;
+    const int64_t oes = MODE == 0 ? 1 : p.lout.estride;
+    uint32_t it = 0;
+    bool ok = true;
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const int buf = it & 1;
+        C2 *st = buf ? stage1 : stage0;
+        const int64_t nxt = tile + gridDim.x;
+        if (tid == 0 && nxt < ntiles) issue(nxt, buf ? stage0 : stage1, &bar[buf ^ 1]);
+        bool mine = mbar_wait_bounded(&bar[buf], (it >> 1) & 1, JT_MBAR_POLL_LIMIT);
+        if (!__syncthreads_and(mine)) {
+            ok = false;
+            break;
+        }
+        const int64_t b0 = tile * S::C;
+        const int64_t b = b0 + c;
+        const bool valid = b < p.nlines;
+        typename V2<T>::t v[S::E];
+        if (MODE == 1) {
+#pragma unroll
+            for (int m = 0; m < S::E; m++) v[m] = st[(t + m * S::TL) * S::C + c];
+        } else {
+#pragma unroll
+            for (int m = 0; m < S::E; m++) v[m] = st[c * L + t + m * S::TL];
+        }
+        __syncthreads();  // every pass-0 read is done before the exchange writes
+        auto xi = [&](int i) { return c * L + (i ^ (((i >> S::LG) ^ c) & (S::G - 1))); };
+        if (MODE == 2) {
+            // last pass to shared memory, then a column-coalesced store
+            auto store_s = [&](int pos, C2 val) { st[xi(pos)] = val; };
+            S::template run<0>(v, t, st, xi, W, store_s);
+            __syncthreads();
+            const int lines = (int)min((int64_t)S::C, p.nlines - b0);
+#pragma unroll 4
+            for (int i = tid; i < S::C * L; i += S::NT) {
+                const int cc = i % S::C, pos = i / S::C;
+                if (cc < lines) {
+                    C2 val = st[cc * L + (pos ^ (((pos >> S::LG) ^ cc) & (S::G - 1)))];
+                    if (do_scale) val = cscale<T>(val, sc);
+                    out[line_off(p.lout, b0 + cc) + (int64_t)pos * oes] = val;
+                }
+            }
+        } else {
+            C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
+            const int64_t j2 = tw ? b % p.tw_inner : 0;
+            auto store = [&](int pos, C2 val) {
+                if (tw) {
+                    int64_t tt = (int64_t)pos * j2;
+                    C2 w = cmul<T>(__ldg(&Whi[tt >> p.tw_lo_bits]), __ldg(&Wlo[tt & lo_mask]));
+                    val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
+                }
+                if (do_scale) val = cscale<T>(val, sc);
+                if (valid) dst[(int64_t)pos * oes] = val;
+            };
+            S::template run<0>(v, t, st, xi, W, store);
+        }
+        // this thread's generic writes to the stage come before the TMA that
+        // refills it two tiles later
+        fence_proxy_async_smem();
+        __syncthreads();
+    }
+    if (!ok) {
+        if (tid == 0) {
+            atomicExch(err, 1);
+            // drain copies still in flight into this CTA's shared memory
+            mbar_wait_bounded(&bar[it & 1], (it >> 1) & 1, JT_MBAR_POLL_LIMIT);
+            if (tile + gridDim.x < ntiles) mbar_wait_bounded(&bar[(it + 1) & 1], ((it + 1) >> 1) & 1, JT_MBAR_POLL_LIMIT);
+        }
+        __syncthreads();
+    }
+}
+
+// Host-side launcher for one (T, L).
 template <typename T, int L> struct StockLaunch {
-    template <int MODE, int SIGN> static void one(const typename V2<T>::t *in, typename V2<T>::t *out, const StockParams &p,
-                                                  const typename V2<T>::t *W, const typename V2<T>::t *Whi,
-                                                  const typename V2<T>::t *Wlo, cudaStream_t s) {
+    typedef typename V2<T>::t C2;
+    template <int MODE, int SIGN> static void one(const C2 *in, C2 *out, const StockParams &p, const CUtensorMap *tmap,
+                                                  const C2 *W, const C2 *Whi, const C2 *Wlo, int *err, int sms,
+                                                  cudaStream_t s) {
         typedef Stockham<T, L, MODE, SIGN> S;
+        int64_t ntiles = (p.nlines + S::C - 1) / S::C;
+        if constexpr (S::PIPE_OK) if (tmap) {
+            static int per_sm = 0;
+            if (!per_sm) {
+                cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)S::PIPE_SMEM);
+                cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     100);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stockham_pipe_kernel<T, L, MODE, SIGN>, S::NT,
+                                                              S::PIPE_SMEM);
+                if (per_sm < 1) per_sm = 1;
+            }
+            int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * per_sm);
+            stockham_pipe_kernel<T, L, MODE, SIGN>
+                <<<(unsigned)grid, S::NT, S::PIPE_SMEM, s>>>(in, out, p, *tmap, W, Whi, Wlo, err);
+            return;
+        }
         static bool attr = false;
         if (!attr) {
             cudaFuncSetAttribute(stockham_kernel<T, L, MODE, SIGN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+            cudaFuncSetAttribute(stockham_kernel<T, L, MODE, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
             attr = true;
         }
-        int64_t grid = (p.nlines + S::C - 1) / S::C;
-        stockham_kernel<T, L, MODE, SIGN><<<(unsigned)grid, S::NT, S::SMEM, s>>>(in, out, p, W, Whi, Wlo);
+        stockham_kernel<T, L, MODE, SIGN><<<(unsigned)ntiles, S::NT, S::SMEM, s>>>(in, out, p, W, Whi, Wlo);
     }
-    static void go(int mode, int sign, const typename V2<T>::t *in, typename V2<T>::t *out, const StockParams &p,
-                   const typename V2<T>::t *W, const typename V2<T>::t *Whi, const typename V2<T>::t *Wlo, cudaStream_t s) {
+    static void go(int mode, int sign, const C2 *in, C2 *out, const StockParams &p, const CUtensorMap *tmap, const C2 *W,
+                   const C2 *Whi, const C2 *Wlo, int *err, int sms, cudaStream_t s) {
         if (mode == 0) {
-            sign < 0 ? one<0, -1>(in, out, p, W, Whi, Wlo, s) : one<0, 1>(in, out, p, W, Whi, Wlo, s);
+            sign < 0 ? one<0, -1>(in, out, p, tmap, W, Whi, Wlo, err, sms, s) : one<0, 1>(in, out, p, tmap, W, Whi, Wlo, err, sms, s);
             return;
         }
         if constexpr (L <= 4096) {  // column modes: C lines of up to 4096 fit one CTA
-            if (mode == 1) sign < 0 ? one<1, -1>(in, out, p, W, Whi, Wlo, s) : one<1, 1>(in, out, p, W, Whi, Wlo, s);
-            else sign < 0 ? one<2, -1>(in, out, p, W, Whi, Wlo, s) : one<2, 1>(in, out, p, W, Whi, Wlo, s);
+            if (mode == 1)
+                sign < 0 ? one<1, -1>(in, out, p, tmap, W, Whi, Wlo, err, sms, s) : one<1, 1>(in, out, p, tmap, W, Whi, Wlo, err, sms, s);
+            else
+                sign < 0 ? one<2, -1>(in, out, p, tmap, W, Whi, Wlo, err, sms, s) : one<2, 1>(in, out, p, tmap, W, Whi, Wlo, err, sms, s);
         }
     }
-    static int lines_per_cta(int mode) { return StockCfg<T>::C(L, mode); }
 };
 
 }  // namespace jt
