@@ -175,7 +175,7 @@ def headline_config(args):
             "sizes": SIZES, "elems_per_size": ELEMS, "global_batch": [ELEMS // n for n in SIZES],
             "parallelism": f"replicas{args.gpus}",
             "l2": "inputs 1 GiB > L2; a 256 MiB buffer is also written before each timed call",
-            "mode": "plain FP32 CUDA cores"}
+            "mode": "plain FP32 CUDA cores", "tma_pipeline": not getattr(args, "no_tma", False)}
 
 
 # ----------------------------------------------------------------------------
@@ -287,6 +287,8 @@ def run_ours(args, world, rank, local):
     import jtransforms_gb300 as J
     from jtransforms_gb300 import _native as N
     torch.cuda.set_device(local)
+    if args.no_tma:
+        N.set_option(N.OPT_TMA_PIPELINE, 0)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -414,6 +416,7 @@ def main():
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 256 MiB per size instead of 1 GiB, no e2e/CPU/other workloads")
     ap.add_argument("--sizes", type=str, default="", help="comma-separated subset of the headline sizes")
+    ap.add_argument("--no-tma", action="store_true", help="use the plain (non-TMA) power-of-two kernel")
     args = ap.parse_args()
     global ELEMS, SIZES
     if args.small:

@@ -131,6 +131,12 @@ int jt_batch_run_per_transform(jt_batch *batch, void *stream);
 int jt_batch_run_graph(jt_batch *batch, void *stream);
 int jt_batch_destroy(jt_batch *batch);
 
+/* Global options --------------------------------------------------------- */
+#define JT_OPT_TMA_PIPELINE 0 /* 1 (default): power-of-two lines use the TMA-pipelined kernel when
+                                 the arrays meet its 16-byte rules; 0: the plain kernel */
+/* Sets a global option; returns the previous value, or JT_EINVAL. */
+int jt_set_option(int option, int value);
+
 /* Diagnostics ------------------------------------------------------------ */
 const char *jt_strerror(int status);
 int jt_last_cuda_error(void);

@@ -45,7 +45,9 @@ SIGNATURES = {
     "jt_last_cuda_error": (_I, []),
     "jt_launch_count": (_L, [_I]),
     "jt_plan_algorithm": (_I, [_P, _I]),
+    "jt_set_option": (_I, [_I, _I]),
 }
+OPT_TMA_PIPELINE = 0
 
 _lib = None
 _lock = threading.Lock()
@@ -170,6 +172,11 @@ class Plan:
                                           int(dist if batch > 1 else ext + (ext & 1)), int(bool(scale)),
                                           ctypes.c_void_p(stream)))
         return a
+
+
+def set_option(option: int, value: int) -> int:
+    """Sets a global library option (OPT_*); returns the previous value."""
+    return load().jt_set_option(option, value)
 
 
 def launch_count(reset: bool = False) -> int:

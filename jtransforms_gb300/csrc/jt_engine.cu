@@ -96,6 +96,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 static EncodeTiledFn g_encode_tiled = nullptr;
+static std::atomic<int> g_opt_tma{1};
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
 
@@ -306,7 +307,7 @@ template <typename T> struct Fft1 {
             const int Cl = stockham_lines_per_cta((int)n, mode, (const T *)nullptr);
             CUtensorMap tm;
             memset(&tm, 0, sizeof(tm));
-            bool pipe = stockham_pipe_ok((int)n, mode, (const T *)nullptr) && ((uintptr_t)in % 16) == 0;
+            bool pipe = g_opt_tma.load() && stockham_pipe_ok((int)n, mode, (const T *)nullptr) && ((uintptr_t)in % 16) == 0;
             if (pipe && mode == 1) {
                 pipe = lin.istride == 1 && lin.inner % Cl == 0 && nlines % lin.inner == 0 &&
                        make_col_tmap(&tm, in, esz, lin.inner, n, nlines / lin.inner, lin.estride, lin.outer, Cl,
@@ -1183,6 +1184,11 @@ const char *jt_strerror(int s) {
 }
 
 int jt_last_cuda_error(void) { return g_last_cuda; }
+
+int jt_set_option(int option, int value) {
+    if (option == JT_OPT_TMA_PIPELINE) return g_opt_tma.exchange(value ? 1 : 0);
+    return JT_EINVAL;
+}
 
 int64_t jt_launch_count(int reset) {
     int64_t v = g_launches;

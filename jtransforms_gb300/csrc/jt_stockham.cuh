@@ -78,13 +78,16 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     static constexpr int REM = 1 << (LOGL % LOGE);
     static constexpr int NPASS = NFULL + (REM > 1 ? 1 : 0);
     static constexpr size_t SMEM = (size_t)C * LP * sizeof(C2);
-    // pipelined kernel: two dense stages of C lines and two mbarriers
-    static constexpr int STAGE = C * L;
+    // pipelined kernel: two stages of C padded lines (TMA fills the first
+    // C*L elements densely; the exchange uses the padded layout) and two
+    // mbarriers
+    static constexpr int STAGE = ((C * LP + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
     static constexpr size_t PIPE_SMEM = 2 * (size_t)STAGE * sizeof(C2) + 16;
     static constexpr bool PIPE_OK = PIPE_SMEM <= 227 * 1024;
-    // XOR swizzle of the exchange: G elements per 128-byte row
-    static constexpr int G = 128 / (int)sizeof(C2);
-    static constexpr int LG = ilog2c(G);
+    // blocks per SM the register budget is sized for (about 24 warps)
+    // (double lines need twice the registers: no cap beyond one block at 256+)
+    static constexpr int MINB = sizeof(T) == 4 ? (NT >= 1024 || NT < 64 ? 1 : (NT >= 512 ? (MODE == 1 ? 2 : 1) : 768 / NT))
+                                               : (NT >= 256 || NT < 64 ? 1 : 384 / NT);
 
     template <int P> struct Pass {
         static constexpr int R = P < NFULL ? E : REM;
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
 #define JT_MBAR_POLL_LIMIT (1u << 22)
 
 template <typename T, int L, int MODE, int SIGN>
-__global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
+__global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L, MODE, SIGN>::MINB)
     stockham_pipe_kernel(const typename V2<T>::t *__restrict__ in, typename V2<T>::t *__restrict__ out, StockParams p,
                          const __grid_constant__ CUtensorMap tmap, const typename V2<T>::t *__restrict__ W,
                          const typename V2<T>::t *__restrict__ Whi, const typename V2<T>::t *__restrict__ Wlo, int *err) {
@@ -290,20 +293,22 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
             for (int m = 0; m < S::E; m++) v[m] = st[c * L + t + m * S::TL];
         }
         __syncthreads();  // every pass-0 read is done before the exchange writes
-        auto xi = [&](int i) { return c * L + (i ^ (((i >> S::LG) ^ c) & (S::G - 1))); };
+        auto xi = [&](int i) { return c * S::LP + pad(i); };
         if (MODE == 2) {
-            // last pass to shared memory, then a column-coalesced store
+            // last pass to shared memory, then a column-coalesced store: the
+            // thread's column cc is fixed, positions advance by NT / C
             auto store_s = [&](int pos, C2 val) { st[xi(pos)] = val; };
             S::template run<0>(v, t, st, xi, W, store_s);
             __syncthreads();
-            const int lines = (int)min((int64_t)S::C, p.nlines - b0);
+            const int cc = tid % S::C;
+            if (b0 + cc < p.nlines) {
+                C2 *o = out + line_off(p.lout, b0 + cc);
+                const C2 *srow = st + cc * S::LP;
 #pragma unroll 4
-            for (int i = tid; i < S::C * L; i += S::NT) {
-                const int cc = i % S::C, pos = i / S::C;
-                if (cc < lines) {
-                    C2 val = st[cc * L + (pos ^ (((pos >> S::LG) ^ cc) & (S::G - 1)))];
+                for (int pos = tid / S::C; pos < L; pos += S::NT / S::C) {
+                    C2 val = srow[pad(pos)];
                     if (do_scale) val = cscale<T>(val, sc);
-                    out[line_off(p.lout, b0 + cc) + (int64_t)pos * oes] = val;
+                    o[(int64_t)pos * oes] = val;
                 }
             }
         } else {
