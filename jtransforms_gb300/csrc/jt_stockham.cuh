@@ -240,7 +240,8 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             const int col0 = (int)((tl - ob * p.tiles_per_col) * S::C);
             constexpr int BR = L < 256 ? L : 256;
             constexpr int XM = sizeof(T) == 4 ? 1 : 2;  // f64 complex = two FLOAT64 in the map
-            mbar_arrive_expect_tx(mb, (uint32_t)(S::STAGE * ESZ));
+            // the boxes bring exactly C * L elements (the stage is larger: padding)
+            mbar_arrive_expect_tx(mb, (uint32_t)(S::C * L * ESZ));
 #pragma unroll 1
             for (int r = 0; r < L; r += BR) tensor3d_g2s(st + r * S::C, &tmap, col0 * XM, r, (int)ob, mb);
         } else if (p.lin.inner == 1 && p.lin.outer == L) {
