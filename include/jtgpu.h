@@ -54,6 +54,7 @@ extern "C" {
 #define JT_ENOMEM (-7)     /* device allocation failed */
 #define JT_ENODEV (-8)     /* no CUDA device */
 #define JT_ETOOBIG (-9)    /* size beyond what this build supports on one GPU */
+#define JT_ESCRATCH (-10)  /* jt_execute_device_noalloc: the transform needs more than the fixed scratch */
 
 /* transform kinds */
 #define JT_FFT 0
@@ -111,6 +112,20 @@ int jt_execute_batch(jt_plan *plan, int op, void *host_array, int64_t array_len,
  * default stream).  Asynchronous: returns after the launches. */
 int jt_execute_device(jt_plan *plan, int op, void *dev_array, int64_t batch,
                       int64_t dist, int scale, void *stream);
+
+/* Complex 1D FFT (JT_COMPLEX_FORWARD / JT_COMPLEX_INVERSE) of `batch`
+ * contiguous transforms from dev_in to dev_out (device memory; they may be the
+ * same array) that allocates nothing.  No counterpart in the reference: it is
+ * for callers that cannot allocate device memory when they transform, such as
+ * code inside CUDA stream capture (cudaMalloc is not allowed there) or with a
+ * fixed memory budget.  Scratch comes from one fixed 32 MiB device array per
+ * GPU: two-pass lengths need n*8 (float) / n*16 (double) bytes of it, so
+ * n <= 2^22 / 2^21 there; Bluestein lengths are refused with JT_ESCRATCH.
+ * Calls share the array, so calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address: make it before any stream
+ * capture.  Asynchronous on `stream` (NULL = the default stream). */
+int jt_execute_device_noalloc(jt_plan *plan, int op, const void *dev_in, void *dev_out, int64_t batch, int scale,
+                              void *stream);
 
 /* Waits for the calling thread's stream; returns JT_ECUDA on a device error. */
 int jt_synchronize(void);

@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_PKG, "libjtgpu.so")
 
 # status codes
 OK, EBADSIZE, ESHORTBUF, ENOTPOW2, ECUDA, ETIMEOUT, EINVAL, ENOMEM, ENODEV, ETOOBIG = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9
+ESCRATCH = -10
 # kinds / precisions / ops
 FFT, DCT, DST, DHT = 0, 1, 2, 3
 FLOAT32, FLOAT64 = 0, 1
@@ -46,6 +47,7 @@ SIGNATURES = {
     "jt_launch_count": (_L, [_I]),
     "jt_plan_algorithm": (_I, [_P, _I]),
     "jt_set_option": (_I, [_I, _I]),
+    "jt_execute_device_noalloc": (_I, [_P, _I, _P, _P, _L, _I, _P]),
 }
 OPT_TMA_PIPELINE = 0
 
@@ -99,7 +101,7 @@ def check(code: int, what: str = ""):
         raise IllegalArgumentException(msg)
     if code == ESHORTBUF:
         raise ArrayIndexOutOfBoundsException(msg)
-    if code in (EINVAL, ETOOBIG):
+    if code in (EINVAL, ETOOBIG, ESCRATCH):
         raise IllegalArgumentException(msg)
     cu = load().jt_last_cuda_error()
     raise IllegalStateException(f"{msg} (cuda error {cu})")

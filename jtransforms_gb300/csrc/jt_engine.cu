@@ -1179,6 +1179,7 @@ const char *jt_strerror(int s) {
         case JT_ENOMEM: return "device out of memory";
         case JT_ENODEV: return "no CUDA device";
         case JT_ETOOBIG: return "size beyond this build's single-GPU limit";
+        case JT_ESCRATCH: return "transform needs more scratch than the fixed 32 MiB no-allocation buffer (or is a Bluestein length)";
     }
     return "unknown status";
 }
@@ -1277,3 +1278,102 @@ int jt_batch_destroy(jt_batch *b) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Complex 1D FFT without any allocation
+//
+// For callers that cannot allocate device memory when they transform: code
+// running while a CUDA stream is being captured into a graph (cudaMalloc is
+// not allowed there), real-time loops with a fixed memory budget, and hosts
+// whose allocator is owned by another framework.  The regular entry points
+// grow a per-thread scratch arena with cudaMalloc on first use of a size;
+// this one takes its scratch from a fixed file-scope device array instead.
+// Each GPU that loads the library holds that array until the process exits.
+//
+// Limit: the scratch is JT_NOALLOC_SCRATCH_BYTES (32 MiB).  Lengths that
+// need the two-pass scheme need one length's worth of complex scratch per
+// transform in flight: n * 8 bytes (float) or n * 16 bytes (double) must fit,
+// so n <= 2^22 (float) / 2^21 (double) there.  Lengths done in one pass need
+// none.  Bluestein lengths are rejected: their scratch would not be bounded
+// by one transform.
+//
+// Sharing: every call uses the same array.  Nothing in it has to start at
+// zero (each transform writes its scratch before reading it), but two calls
+// whose kernels overlap on the GPU (different streams, or different host
+// threads on one device) race on it: order them on one stream.
+//
+// Set-up: the first call on a device looks up the array's device address
+// there (cudaGetSymbolAddress, with that device current) and keeps it.  Make
+// that first call before any stream capture begins.
+// ===========================================================================
+#define JT_NOALLOC_SCRATCH_BYTES (32u << 20)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[JT_NOALLOC_SCRATCH_BYTES];
+static void *g_noalloc_addr[64];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch(void **out) {
+    int dev = 0;
+    JT_CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return JT_EINVAL;
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            g_last_cuda = (int)e;
+            return JT_ECUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return JT_OK;
+}
+
+template <typename T>
+static int noalloc_run(jt_plan *p, int op, const void *in, void *out, int64_t batch, int scale, cudaStream_t s) {
+    typedef typename V2<T>::t C2;
+    PlanImpl<T> *im = (PlanImpl<T> *)p->impl;
+    const int64_t n = p->dims[0];
+    std::lock_guard<std::mutex> g(im->mu);
+    auto it = im->fft.find(n);
+    if (it == im->fft.end()) return JT_EINVAL;  // tables are built by jt_plan_create
+    Fft1<T> *f = it->second.get();
+    if (f->algo == ALG_BLUESTEIN) return JT_ESCRATCH;
+    const int64_t per = f->algo == ALG_TWOPASS ? n * (int64_t)sizeof(C2) : 0;
+    if (per > (int64_t)JT_NOALLOC_SCRATCH_BYTES) return JT_ESCRATCH;
+    void *scratch = nullptr;
+    JT_TRY(noalloc_scratch(&scratch));
+    const int64_t sub = per ? std::max<int64_t>(1, (int64_t)JT_NOALLOC_SCRATCH_BYTES / per) : batch;
+    const int sign = op == JT_COMPLEX_FORWARD ? -1 : 1;
+    const double sc = (op == JT_COMPLEX_INVERSE && scale) ? 1.0 / (double)n : 1.0;
+    const C2 *src = (const C2 *)in;
+    C2 *dst = (C2 *)out;
+    for (int64_t b = 0; b < batch; b += sub) {
+        const int64_t cb = std::min(sub, batch - b);
+        Arena ar;
+        ar.base = (char *)scratch;
+        ar.cap = JT_NOALLOC_SCRATCH_BYTES;
+        Ctx c;
+        c.s = s;
+        c.ws = &ar;
+        c.dry = true;  // size check first: nothing may spill past the array
+        JT_TRY(f->exec(c, src + b * n, n, dst + b * n, n, cb, sign, sc));
+        if (ar.peak > ar.cap) return JT_ESCRATCH;
+        ar.used = ar.peak = 0;
+        c.dry = false;
+        JT_TRY(f->exec(c, src + b * n, n, dst + b * n, n, cb, sign, sc));
+    }
+    JT_CU(cudaGetLastError());
+    return JT_OK;
+}
+
+extern "C" int jt_execute_device_noalloc(jt_plan *p, int op, const void *dev_in, void *dev_out, int64_t batch, int scale,
+                                         void *stream) {
+    if (!p || !dev_in || !dev_out || batch < 0) return JT_EINVAL;
+    if (p->kind != JT_FFT || p->nd != 1 || (op != JT_COMPLEX_FORWARD && op != JT_COMPLEX_INVERSE)) return JT_EINVAL;
+    if (batch == 0) return JT_OK;
+    const size_t esz = p->prec == JT_FLOAT32 ? 8 : 16;
+    if (((uintptr_t)dev_in % esz) || ((uintptr_t)dev_out % esz)) return JT_EINVAL;
+    if (p->prec == JT_FLOAT32) return noalloc_run<float>(p, op, dev_in, dev_out, batch, scale, (cudaStream_t)stream);
+    return noalloc_run<double>(p, op, dev_in, dev_out, batch, scale, (cudaStream_t)stream);
+}
