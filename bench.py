@@ -289,6 +289,8 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(local)
     if args.no_tma:
         N.set_option(N.OPT_TMA_PIPELINE, 0)
+    if args.direct_max:
+        N.set_option(N.OPT_DIRECT_MAX_F32, args.direct_max)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -417,6 +419,7 @@ def main():
                     help="profiling case: 256 MiB per size instead of 1 GiB, no e2e/CPU/other workloads")
     ap.add_argument("--sizes", type=str, default="", help="comma-separated subset of the headline sizes")
     ap.add_argument("--no-tma", action="store_true", help="use the plain (non-TMA) power-of-two kernel")
+    ap.add_argument("--direct-max", type=int, default=0, help="longest float length done in one pass")
     args = ap.parse_args()
     global ELEMS, SIZES
     if args.small:

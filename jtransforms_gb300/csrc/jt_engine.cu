@@ -97,6 +97,8 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 static EncodeTiledFn g_encode_tiled = nullptr;
 static std::atomic<int> g_opt_tma{1};
+static std::atomic<int> g_opt_direct_max_f32{16384};
+static std::atomic<int> g_opt_direct_max_f64{8192};
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
 
@@ -207,6 +209,9 @@ template <typename T> struct Fft1 {
     // register-resident power-of-two kernel (jt_stockham.cuh): row mode up to
     // reg_rows_max, column modes up to 4096
     static int64_t reg_rows_max() { return sizeof(T) == 4 ? 16384 : 8192; }
+    static int64_t one_pass_max() {
+        return std::min<int64_t>(reg_rows_max(), sizeof(T) == 4 ? g_opt_direct_max_f32.load() : g_opt_direct_max_f64.load());
+    }
     static bool reg_ok(int64_t n) { return is_pow2(n) && n >= 16 && n <= reg_rows_max(); }
     static bool direct_ok(int64_t n) { return reg_ok(n) || generic_ok(n); }
     bool reg = false;
@@ -227,7 +232,7 @@ template <typename T> struct Fft1 {
         f->n = n;
         if (n == 1) {
             f->algo = ALG_TRIVIAL;
-        } else if (direct_ok(n)) {
+        } else if (direct_ok(n) && (!is_pow2(n) || n <= one_pass_max())) {
             f->algo = ALG_DIRECT;
             f->reg = reg_ok(n);
             if (!f->reg) f->radix = direct_radices(n);
@@ -1188,6 +1193,8 @@ int jt_last_cuda_error(void) { return g_last_cuda; }
 
 int jt_set_option(int option, int value) {
     if (option == JT_OPT_TMA_PIPELINE) return g_opt_tma.exchange(value ? 1 : 0);
+    if (option == JT_OPT_DIRECT_MAX_F32) return g_opt_direct_max_f32.exchange(value);
+    if (option == JT_OPT_DIRECT_MAX_F64) return g_opt_direct_max_f64.exchange(value);
     return JT_EINVAL;
 }
 

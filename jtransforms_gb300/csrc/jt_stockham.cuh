@@ -53,7 +53,7 @@ template <typename T> struct StockCfg {
     // lines per CTA for the column modes: 128-byte row segments when the
     // line is short, at least one 32-byte sector when it is long
     static constexpr int cols_C(int L) {
-        return sizeof(T) == 4 ? (L <= 512 ? 16 : (8192 / L < 4 ? 4 : 8192 / L))
+        return sizeof(T) == 4 ? (L <= 512 ? 16 : 8192 / L)
                               : (L <= 256 ? 8 : (4096 / L < 2 ? 2 : 4096 / L));
     }
     static constexpr int C(int L, int mode) { return mode == 0 ? rows_C(L) : cols_C(L); }
@@ -97,11 +97,29 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
         static constexpr bool LAST = P == NPASS - 1;
     };
 
-    // Butterflies of pass P on the thread's registers; non-last passes write
-    // their outputs to shared memory at xs[xi(index)] and read the next
-    // pass's inputs back.
+    // Twiddles of pass P for this thread: NB butterflies x (R-1) factors.
+    template <int P> struct Tw {
+        static constexpr int N = Pass<P>::NS > 1 ? Pass<P>::NB * (Pass<P>::R - 1) : 1;
+    };
+    template <int P> static __device__ __forceinline__ void load_tw(int t, const C2 *__restrict__ W, C2 (&tw)[Tw<P>::N]) {
+        typedef Pass<P> PP;
+        if constexpr (PP::NS > 1) {
+#pragma unroll
+            for (int q = 0; q < PP::NB; q++) {
+                const int jm = (t + q * TL) & (PP::NS - 1);
+#pragma unroll
+                for (int k = 1; k < PP::R; k++) tw[q * (PP::R - 1) + k - 1] = __ldg(&W[(jm * k) << PP::SHIFT]);
+            }
+        }
+    }
+
+    // Butterflies of pass P on the thread's registers, with its twiddles
+    // already in `tw`; non-last passes write their outputs to shared memory
+    // at xs[xi(index)], load the next pass's twiddles (in flight during the
+    // exchange) and read the next pass's inputs back.
     template <int P, typename Store, typename XIdx>
-    static __device__ __forceinline__ void run(C2 (&v)[E], int t, C2 *xs, XIdx &xi, const C2 *__restrict__ W, Store &store) {
+    static __device__ __forceinline__ void run(C2 (&v)[E], const C2 (&tw)[Tw<P>::N], int t, C2 *xs, XIdx &xi,
+                                               const C2 *__restrict__ W, Store &store) {
         typedef Pass<P> PP;
 #pragma unroll
         for (int q = 0; q < PP::NB; q++) {
@@ -113,7 +131,7 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
             if (PP::NS > 1) {
 #pragma unroll
                 for (int k = 1; k < PP::R; k++) {
-                    C2 w = __ldg(&W[(jm * k) << PP::SHIFT]);
+                    C2 w = tw[q * (PP::R - 1) + k - 1];
                     u[k] = SIGN < 0 ? cmul<T>(u[k], w) : cmulc<T>(u[k], w);
                 }
             }
@@ -126,12 +144,20 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
             }
         }
         if constexpr (!PP::LAST) {
+            C2 tw2[Tw<P + 1>::N];
+            load_tw<P + 1>(t, W, tw2);
             __syncthreads();
 #pragma unroll
             for (int m = 0; m < E; m++) v[m] = xs[xi(t + m * TL)];
             __syncthreads();
-            run<P + 1>(v, t, xs, xi, W, store);
+            run<P + 1>(v, tw2, t, xs, xi, W, store);
         }
+    }
+
+    template <typename Store, typename XIdx>
+    static __device__ __forceinline__ void run_all(C2 (&v)[E], int t, C2 *xs, XIdx &xi, const C2 *__restrict__ W, Store &store) {
+        C2 tw0[Tw<0>::N];
+        run<0>(v, tw0, t, xs, xi, W, store);
     }
 };
 
@@ -182,23 +208,23 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
     }
 
     C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
-    const int64_t oes = MODE == 0 ? 1 : p.lout.estride;
+    const int oes32 = MODE == 0 ? 1 : (int)p.lout.estride;
     const bool tw = p.tw_n != 0;
-    const int64_t j2 = tw ? b % p.tw_inner : 0;
-    const int64_t lo_mask = ((int64_t)1 << p.tw_lo_bits) - 1;
+    const int j2 = tw ? (int)(b % p.tw_inner) : 0;
+    const int lo_mask = (1 << p.tw_lo_bits) - 1;
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
     auto store = [&](int pos, C2 val) {
         if (tw) {
-            int64_t tt = (int64_t)pos * j2;
+            const int tt = pos * j2;  // < tw_n <= 2^26
             C2 w = cmul<T>(__ldg(&Whi[tt >> p.tw_lo_bits]), __ldg(&Wlo[tt & lo_mask]));
             val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
         }
         if (do_scale) val = cscale<T>(val, sc);
-        if (valid) dst[(int64_t)pos * oes] = val;
+        if (valid) dst[(int64_t)pos * oes32] = val;
     };
     auto xi = [&](int i) { return c * S::LP + pad(i); };
-    S::template run<0>(v, t, sm, xi, W, store);
+    S::run_all(v, t, sm, xi, W, store);
 }
 
 // ---------------------------------------------------------------------------
@@ -266,10 +292,10 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
     if (tid == 0 && tile < ntiles) issue(tile, stage0, &bar[0]);
 
     const bool tw = p.tw_n != 0;
-    const int64_t lo_mask = ((int64_t)1 << p.tw_lo_bits) - 1;
+    const int lo_mask = (1 << p.tw_lo_bits) - 1;
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
-    const int64_t oes = MODE == 0 ? 1 : p.lout.estride;
+    const int oes32 = MODE == 0 ? 1 : (int)p.lout.estride;
     uint32_t it = 0;
     bool ok = true;
     for (; tile < ntiles; tile += gridDim.x, ++it) {
@@ -299,7 +325,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             // last pass to shared memory, then a column-coalesced store: the
             // thread's column cc is fixed, positions advance by NT / C
             auto store_s = [&](int pos, C2 val) { st[xi(pos)] = val; };
-            S::template run<0>(v, t, st, xi, W, store_s);
+            S::run_all(v, t, st, xi, W, store_s);
             __syncthreads();
             const int cc = tid % S::C;
             if (b0 + cc < p.nlines) {
@@ -309,22 +335,22 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
                 for (int pos = tid / S::C; pos < L; pos += S::NT / S::C) {
                     C2 val = srow[pad(pos)];
                     if (do_scale) val = cscale<T>(val, sc);
-                    o[(int64_t)pos * oes] = val;
+                    o[(int64_t)pos * oes32] = val;
                 }
             }
         } else {
             C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
-            const int64_t j2 = tw ? b % p.tw_inner : 0;
+            const int j2 = tw ? (int)(b % p.tw_inner) : 0;
             auto store = [&](int pos, C2 val) {
                 if (tw) {
-                    int64_t tt = (int64_t)pos * j2;
+                    const int tt = pos * j2;  // < tw_n <= 2^26
                     C2 w = cmul<T>(__ldg(&Whi[tt >> p.tw_lo_bits]), __ldg(&Wlo[tt & lo_mask]));
                     val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
                 }
                 if (do_scale) val = cscale<T>(val, sc);
-                if (valid) dst[(int64_t)pos * oes] = val;
+                if (valid) dst[(int64_t)pos * oes32] = val;
             };
-            S::template run<0>(v, t, st, xi, W, store);
+            S::run_all(v, t, st, xi, W, store);
         }
         // this thread's generic writes to the stage come before the TMA that
         // refills it two tiles later
