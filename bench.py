@@ -291,6 +291,8 @@ def run_ours(args, world, rank, local):
         N.set_option(N.OPT_TMA_PIPELINE, 0)
     if args.direct_max:
         N.set_option(N.OPT_DIRECT_MAX_F32, args.direct_max)
+    if args.no_colpass:
+        N.set_option(N.OPT_COLUMN_KERNEL, 0)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -420,6 +422,7 @@ def main():
     ap.add_argument("--sizes", type=str, default="", help="comma-separated subset of the headline sizes")
     ap.add_argument("--no-tma", action="store_true", help="use the plain (non-TMA) power-of-two kernel")
     ap.add_argument("--direct-max", type=int, default=0, help="longest float length done in one pass")
+    ap.add_argument("--no-colpass", action="store_true", help="column passes on the tile-pipelined kernel")
     args = ap.parse_args()
     global ELEMS, SIZES
     if args.small:
