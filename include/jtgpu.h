@@ -152,8 +152,8 @@ int jt_batch_destroy(jt_batch *batch);
 #define JT_OPT_DIRECT_MAX_F32 1 /* longest power-of-two float length done in one pass (default 16384);
                                    longer lengths use two passes.  Read when a plan is created. */
 #define JT_OPT_DIRECT_MAX_F64 2 /* the same for double (default 8192) */
-#define JT_OPT_COLUMN_KERNEL 3  /* 1 (default): column passes use the line-group kernel with TMA tensor
-                                   loads and stores; 0: the tile-pipelined kernel */
+#define JT_OPT_COLUMN_KERNEL 3  /* 0 (default): column passes use the tile-pipelined kernel; 1: the
+                                   line-group kernel with swizzled TMA tensor loads and stores */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 

@@ -97,7 +97,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 static EncodeTiledFn g_encode_tiled = nullptr;
 static std::atomic<int> g_opt_tma{1};
-static std::atomic<int> g_opt_colpass{1};
+static std::atomic<int> g_opt_colpass{0};
 static std::atomic<int> g_opt_direct_max_f32{16384};
 static std::atomic<int> g_opt_direct_max_f64{8192};
 static std::once_flag g_dev_once;
@@ -299,7 +299,7 @@ template <typename T> struct Fft1 {
     // DIRECT pass over `nlines` lines with arbitrary layouts.
     int exec_direct(Ctx &ctx, const C2 *in, C2 *out, int64_t nlines, const Layout &lin, const Layout &lout, int sign,
                     double scale, int64_t tw_n = 0, int64_t tw_inner = 1, const C2 *Whi_ = nullptr, const C2 *Wlo_ = nullptr,
-                    int tw_lo_bits = 0) const {
+                    int tw_lo_bits = 0, int hint_discard_in = 0, int hint_stream_out = 1) const {
         if (nlines <= 0) return JT_OK;
         if (reg) {
             int mode = -1;
@@ -318,6 +318,8 @@ template <typename T> struct Fft1 {
             sp.tw_n = tw_n;
             sp.tw_inner = tw_inner;
             sp.tw_lo_bits = tw_lo_bits;
+            sp.discard_in = hint_discard_in;
+            sp.stream_out = hint_stream_out;
             if (ctx.dry) return JT_OK;
             const int esz = (int)sizeof(C2);
             // column passes: group-per-line kernel with TMA tensor load/store
@@ -422,9 +424,9 @@ template <typename T> struct Fft1 {
                 for (int64_t b = 0; b < batch; b += chunk) {
                     int64_t cb = std::min(chunk, batch - b);
                     Layout lai = {n2, din, 1, n2}, lao = {n2, n, 1, n2};
-                    JT_TRY(pa->exec_direct(ctx, in + b * din, tmp, cb * n2, lai, lao, sign, 1.0, n, n2, Whi, Wlo, lo_bits));
+                    JT_TRY(pa->exec_direct(ctx, in + b * din, tmp, cb * n2, lai, lao, sign, 1.0, n, n2, Whi, Wlo, lo_bits, 0, 0));
                     Layout lbi = {n1, n, n2, 1}, lbo = {n1, dout, 1, n1};
-                    JT_TRY(pb->exec_direct(ctx, tmp, out + b * dout, cb * n1, lbi, lbo, sign, scale));
+                    JT_TRY(pb->exec_direct(ctx, tmp, out + b * dout, cb * n1, lbi, lbo, sign, scale, 0, 1, nullptr, nullptr, 0, 1, 1));
                 }
                 return JT_OK;
             }

@@ -40,6 +40,8 @@ struct StockParams {
     int64_t tw_n, tw_inner;  // four-step output twiddle w_{tw_n}^{pos * (b % tw_inner)}; tw_n = 0: none
     int tw_lo_bits;
     int64_t tiles_per_col;   // MODE 1 pipe: column tiles per outer block (inner / C)
+    int discard_in;          // MODE 2 pipe: the input is a dead intermediate (drop it from L2)
+    int stream_out;          // outputs are not re-read soon: streaming stores
 };
 
 template <typename T> __device__ __forceinline__ T param_scale(const StockParams &p) {
@@ -86,7 +88,7 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     static constexpr bool PIPE_OK = PIPE_SMEM <= 227 * 1024;
     // blocks per SM the register budget is sized for (about 24 warps)
     // (double lines need twice the registers: no cap beyond one block at 256+)
-    static constexpr int MINB = sizeof(T) == 4 ? (NT >= 1024 || NT < 64 ? 1 : (NT >= 512 ? (MODE == 1 ? 2 : 1) : 768 / NT))
+    static constexpr int MINB = sizeof(T) == 4 ? (NT >= 512 || NT < 64 ? 1 : 768 / NT)
                                                : (NT >= 256 || NT < 64 ? 1 : 384 / NT);
 
     template <int P> struct Pass {
@@ -263,7 +265,10 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
     const int64_t ntiles = (p.nlines + S::C - 1) / S::C;
     constexpr uint32_t ESZ = sizeof(C2);
 
-    // Issues the copies of tile `tl` into `st`, completing on `mb`.
+    // Issues the copies of tile `tl` into `st`, completing on `mb`.  Input
+    // read once (the caller's array in MODE 0/1, the dead intermediate in
+    // MODE 2) is marked evict-first so the two-pass intermediate keeps L2.
+    const uint64_t pol = policy_evict_first();
     auto issue = [&](int64_t tl, C2 *st, uint64_t *mb) {
         const int64_t b0 = tl * S::C;
         const int lines = (int)min((int64_t)S::C, p.nlines - b0);
@@ -276,15 +281,16 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             // the boxes bring exactly C * L elements (the stage is larger: padding)
             mbar_arrive_expect_tx(mb, (uint32_t)(S::C * L * ESZ));
 #pragma unroll 1
-            for (int r = 0; r < L; r += BR) tensor3d_g2s(st + r * S::C, &tmap, col0 * XM, r, (int)ob, mb);
+            for (int r = 0; r < L; r += BR) tensor3d_g2s_hint(st + r * S::C, &tmap, col0 * XM, r, (int)ob, mb, pol);
         } else if (p.lin.inner == 1 && p.lin.outer == L) {
             // C consecutive contiguous rows: one copy
             mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
-            bulk_g2s(st, in + b0 * L, (uint32_t)(lines * L * ESZ), mb);
+            bulk_g2s_hint(st, in + b0 * L, (uint32_t)(lines * L * ESZ), mb, pol);
         } else {
             mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
 #pragma unroll 1
-            for (int cc = 0; cc < lines; cc++) bulk_g2s(st + cc * L, in + line_off(p.lin, b0 + cc), (uint32_t)(L * ESZ), mb);
+            for (int cc = 0; cc < lines; cc++)
+                bulk_g2s_hint(st + cc * L, in + line_off(p.lin, b0 + cc), (uint32_t)(L * ESZ), mb, pol);
         }
     };
 
@@ -318,6 +324,15 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         const int64_t b0 = tile * S::C;
         const int64_t b = b0 + c;
         const bool valid = b < p.nlines;
+        if (MODE == 2 && p.discard_in) {
+            // the intermediate rows are now in shared memory and dead in L2
+            const int lines = (int)min((int64_t)S::C, p.nlines - b0);
+            constexpr int PER_LINE = L * (int)ESZ / 128;
+            for (int i = tid; i < lines * PER_LINE; i += S::NT) {
+                const int cc = i / PER_LINE, k = i - cc * PER_LINE;
+                discard_l2_line(reinterpret_cast<const unsigned char *>(in + line_off(p.lin, b0 + cc)) + k * 128);
+            }
+        }
         typename V2<T>::t v[S::E];
         if (MODE == 1) {
 #pragma unroll
@@ -342,20 +357,43 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
                 for (int pos = tid / S::C; pos < L; pos += S::NT / S::C) {
                     C2 val = srow[pad(pos)];
                     if (do_scale) val = cscale<T>(val, sc);
-                    o[(int64_t)pos * oes32] = val;
+                    if (p.stream_out) __stcs(&o[(int64_t)pos * oes32], val);
+                    else o[(int64_t)pos * oes32] = val;
                 }
             }
         } else {
             C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
             const int j2 = tw ? (int)(b % p.tw_inner) : 0;
-            auto store = [&](int pos, C2 val, int) {
+            // Four-step twiddle w^{pos*j2}: the last pass writes pos = t + TL*m,
+            // m = q + k*NB for output slot q*R + k, so
+            // w^{pos*j2} = (w^{t*j2} w^{(m&3)*TL*j2}) * w^{(m>>2)*4*TL*j2}:
+            // seven table lookups per thread instead of one per output.
+            typedef typename S::template Pass<S::NPASS - 1> LP_;
+            auto twv = [&](int x) { return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & lo_mask])); };
+            C2 bl[4], gh[4];
+            auto store = [&](int pos, C2 val, int slot) {
                 if (tw) {
-                    const int tt = pos * j2;  // < tw_n <= 2^26
-                    C2 w = cmul<T>(__ldg(&Whi[tt >> p.tw_lo_bits]), __ldg(&Wlo[tt & lo_mask]));
+                    if (slot == 0) {
+                        const int g = S::TL * j2;
+                        C2 base = twv(t * j2);
+                        bl[0] = base;
+                        bl[1] = cmul<T>(base, twv(g));
+                        bl[2] = cmul<T>(base, twv(2 * g));
+                        bl[3] = cmul<T>(base, twv(3 * g));
+                        gh[0] = mk<T>(1, 0);
+                        gh[1] = twv(4 * g);
+                        gh[2] = twv(8 * g);
+                        gh[3] = twv(12 * g);
+                    }
+                    const int m = slot / LP_::R + (slot % LP_::R) * LP_::NB;
+                    C2 w = m < 4 ? bl[m & 3] : cmul<T>(bl[m & 3], gh[m >> 2]);
                     val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
                 }
                 if (do_scale) val = cscale<T>(val, sc);
-                if (valid) dst[(int64_t)pos * oes32] = val;
+                if (valid) {
+                    if (p.stream_out) __stcs(&dst[(int64_t)pos * oes32], val);
+                    else dst[(int64_t)pos * oes32] = val;
+                }
             };
             S::run_all(v, t, st, xi, W, store);
         }

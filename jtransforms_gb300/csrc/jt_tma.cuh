@@ -87,3 +87,41 @@ __device__ __forceinline__ void named_barrier(int id, int count) {
 }
 
 }  // namespace jt
+
+namespace jt {
+
+// L2 eviction-priority policies (createpolicy) for cache-hinted copies.
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ void bulk_g2s_hint(void *dst, const void *src, uint32_t bytes, uint64_t *bar, uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+        : "memory");
+}
+
+__device__ __forceinline__ void tensor3d_g2s_hint(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar,
+                                                  uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, %3, %4}], "
+        "[%5], %6;" ::"r"(smem_addr(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar)), "l"(pol)
+        : "memory");
+}
+
+// Drops a 128-byte L2 line without writing it back (its data is dead).
+__device__ __forceinline__ void discard_l2_line(const void *p) {
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
+
+}  // namespace jt
