@@ -149,7 +149,7 @@ int jt_batch_destroy(jt_batch *batch);
 /* Global options --------------------------------------------------------- */
 #define JT_OPT_TMA_PIPELINE 0 /* 1 (default): power-of-two lines use the TMA-pipelined kernel when
                                  the arrays meet its 16-byte rules; 0: the plain kernel */
-#define JT_OPT_DIRECT_MAX_F32 1 /* longest power-of-two float length done in one pass (default 16384);
+#define JT_OPT_DIRECT_MAX_F32 1 /* longest power-of-two float length done in one pass (default 8192);
                                    longer lengths use two passes.  Read when a plan is created. */
 #define JT_OPT_DIRECT_MAX_F64 2 /* the same for double (default 8192) */
 #define JT_OPT_COLUMN_KERNEL 3  /* 0 (default): column passes use the tile-pipelined kernel; 1: the

@@ -98,7 +98,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
 static EncodeTiledFn g_encode_tiled = nullptr;
 static std::atomic<int> g_opt_tma{1};
 static std::atomic<int> g_opt_colpass{0};
-static std::atomic<int> g_opt_direct_max_f32{16384};
+static std::atomic<int> g_opt_direct_max_f32{8192};
 static std::atomic<int> g_opt_direct_max_f64{8192};
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
@@ -1157,17 +1157,18 @@ int jt_plan_set_mode(jt_plan *p, int mode) {
 
 int jt_plan_algorithm(const jt_plan *p, int axis) {
     if (!p || axis < 0 || axis >= p->nd) return JT_EINVAL;
-    int64_t n = p->dims[axis];
-    if (n == 1) return ALG_TRIVIAL;
+    const int64_t n = p->dims[axis];
     if (p->prec == JT_FLOAT32) {
-        if (Fft1<float>::direct_ok(n)) return ALG_DIRECT;
-    } else if (Fft1<double>::direct_ok(n)) {
-        return ALG_DIRECT;
+        PlanImpl<float> *im = (PlanImpl<float> *)p->impl;
+        std::lock_guard<std::mutex> g(im->mu);
+        auto it = im->fft.find(n);
+        if (it != im->fft.end()) return it->second->algo;
+    } else {
+        PlanImpl<double> *im = (PlanImpl<double> *)p->impl;
+        std::lock_guard<std::mutex> g(im->mu);
+        auto it = im->fft.find(n);
+        if (it != im->fft.end()) return it->second->algo;
     }
-    PlanImpl<float> *imf = p->prec == JT_FLOAT32 ? (PlanImpl<float> *)p->impl : nullptr;
-    PlanImpl<double> *imd = p->prec == JT_FLOAT64 ? (PlanImpl<double> *)p->impl : nullptr;
-    if (imf && imf->fft.count(n)) return imf->fft.at(n)->algo;
-    if (imd && imd->fft.count(n)) return imd->fft.at(n)->algo;
     return JT_EINVAL;
 }
 
