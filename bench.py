@@ -279,7 +279,92 @@ def other_workloads(args, peak, flush, stream):
     h3 = J.DoubleDHT_3D(128, 128, 128)
     measure("c3c_DoubleDHT_3D_128_forward", h3.plan, N.FORWARD, x, 1, N3, False,
             2.5 * N3 * math.log2(N3), 2 * 8 * N3, "2.5N log2N")
+    del x
+    out["c5_mixed_batch_10000"] = mixed_batch(args, rng, flush, stream)
     return out
+
+
+def batch_descriptors(count, rng):
+    """(kind, n) of the mixed batch: sizes log-uniform in [16, 65536] redrawn
+    into classes (40% powers of two, 40% 2^a 3^b 5^c 7^d, 20% primes); kinds
+    50% FloatFFT_1D.complexForward, 25% FloatFFT_1D.realForward, 25%
+    DoubleDCT_1D.forward(scale=true)."""
+    lo, hi = 16, 65536
+    smooth = sorted({2 ** a * 3 ** b * 5 ** c * 7 ** d for a in range(17) for b in range(11) for c in range(8)
+                     for d in range(7) if lo <= 2 ** a * 3 ** b * 5 ** c * 7 ** d <= hi})
+    sieve = np.ones(hi + 200, bool)
+    sieve[:2] = False
+    for i in range(2, int((hi + 200) ** 0.5) + 1):
+        if sieve[i]:
+            sieve[i * i::i] = False
+    primes = np.nonzero(sieve)[0]
+    primes = primes[(primes >= lo) & (primes <= hi)]
+    smooth = np.array(smooth)
+    out = []
+    for _ in range(count):
+        x = math.exp(rng.uniform(math.log(lo), math.log(hi)))
+        c = rng.uniform()
+        if c < 0.4:
+            n = 2 ** int(round(math.log2(x)))
+        elif c < 0.8:
+            n = int(smooth[np.argmin(np.abs(smooth - x))])
+        else:
+            n = int(primes[np.argmin(np.abs(primes - x))])
+        k = rng.uniform()
+        kind = "cf" if k < 0.5 else ("rf" if k < 0.75 else "dct")
+        out.append((kind, n))
+    return out
+
+
+def mixed_batch(args, rng, flush, stream):
+    import torch
+    from jtransforms_gb300 import _native as N
+    desc = batch_descriptors(10000, rng)
+    plans = {}
+    f32_off, f64_off, items_spec = 0, 0, []
+    for kind, n in desc:
+        key = (kind, n)
+        if key not in plans:
+            if kind == "dct":
+                plans[key] = N.Plan(N.DCT, N.FLOAT64, [n])
+            else:
+                plans[key] = N.Plan(N.FFT, N.FLOAT32, [n])
+        ext = 2 * n if kind == "cf" else n
+        ext = (ext + 3) & ~3  # keep every array 16-byte aligned
+        if kind == "dct":
+            items_spec.append((key, f64_off, ext))
+            f64_off += ext
+        else:
+            items_spec.append((key, f32_off, ext))
+            f32_off += ext
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    b32 = torch.rand(max(f32_off, 1), dtype=torch.float32, device="cuda", generator=g) * 2 - 1
+    b64 = torch.rand(max(f64_off, 1), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    p32, p64 = b32.clone(), b64.clone()
+    opc = {"cf": N.COMPLEX_FORWARD, "rf": N.REAL_FORWARD, "dct": N.FORWARD}
+    items = []
+    flops = 0.0
+    for (kind, n), off, ext in items_spec:
+        buf = b64 if kind == "dct" else b32
+        ptr = buf.data_ptr() + off * buf.element_size()
+        items.append((plans[(kind, n)], opc[kind], ptr, kind == "dct"))
+        flops += (5.0 if kind == "cf" else 2.5) * n * math.log2(n)
+    batch = N.Batch(items)
+
+    def restore(i):
+        b32.copy_(p32)
+        b64.copy_(p64)
+
+    steps, warm = max(args.steps, 3), max(args.warmup, 2)
+    t_graph = timed_calls([lambda: batch.run_graph()], restore, flush, steps, warm, stream)[0]
+    t_pers = timed_calls([lambda: batch.run()], restore, flush, steps, warm, stream)[0]
+    t_each = timed_calls([lambda: batch.run_per_transform()], restore, flush, max(2, steps // 2), 1, stream)[0]
+    mg, mp, me = statistics.median(t_graph), statistics.median(t_pers), statistics.median(t_each)
+    return {"value": len(desc) / (mg * 1e-3), "unit": "transforms/s", "ms": mg,
+            "persistent_launch_ms": mp, "per_transform_launches_ms": me,
+            "speedup_vs_per_transform": me / mg, "GFLOP/s": flops / (mg * 1e-3) / 1e9,
+            "distinct_plans": len(plans), "transforms": len(desc),
+            "flops": "5N log2N complex, 2.5N log2N real and DCT"}
 
 
 def run_ours(args, world, rank, local):

@@ -183,3 +183,52 @@ def set_option(option: int, value: int) -> int:
 
 def launch_count(reset: bool = False) -> int:
     return load().jt_launch_count(int(reset))
+
+
+class Batch:
+    """Many 1D transforms of different plans run as one persistent launch
+    (jt_batch_create / jt_batch_run / jt_batch_run_graph).
+
+    `items` is a list of (Plan, op, tensor_or_device_ptr, scale).  Arrays
+    are device memory; the batch records their addresses, so they must stay
+    alive and in place while the batch is used."""
+
+    def __init__(self, items):
+        self._lib = load()
+        self._keep = items
+        n = len(items)
+        plans = (ctypes.c_void_p * n)(*[it[0].handle.value for it in items])
+        ops = (ctypes.c_int * n)(*[int(it[1]) for it in items])
+        ptrs = (ctypes.c_void_p * n)(*[(it[2].data_ptr() if hasattr(it[2], "data_ptr") else int(it[2])) for it in items])
+        scales = (ctypes.c_int * n)(*[int(bool(it[3])) for it in items])
+        h = ctypes.c_void_p()
+        check(self._lib.jt_batch_create(n, plans, ops, ptrs, scales, ctypes.byref(h)))
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self._lib.jt_batch_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    @staticmethod
+    def _stream(stream):
+        if stream is None:
+            import torch
+            return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        return ctypes.c_void_p(int(stream))
+
+    def run(self, stream=None):
+        """One persistent launch (asynchronous)."""
+        check(self._lib.jt_batch_run(self.handle, self._stream(stream)))
+
+    def run_graph(self, stream=None):
+        """The same launch captured once into a CUDA graph, then replayed."""
+        check(self._lib.jt_batch_run_graph(self.handle, self._stream(stream)))
+
+    def run_per_transform(self, stream=None):
+        """The baseline: each transform's own launches, one after another."""
+        check(self._lib.jt_batch_run_per_transform(self.handle, self._stream(stream)))

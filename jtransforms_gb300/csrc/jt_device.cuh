@@ -306,14 +306,15 @@ __device__ void pass_generic(const C2 *__restrict__ src, C2 *__restrict__ dst, i
 
 // W: e^{-2 pi i t/L}, t < L.  Whi/Wlo: two-level table of the four-step post
 // twiddle, e^{-2 pi i t/tw_n} = Whi[t >> lo_bits] * Wlo[t & mask].
+// Tile `blk` of a generic line pass, run by the calling CTA with its shared
+// memory at `smem_raw` (2 * C * padded L elements).
 template <int SIGN, typename T>
-__global__ void __launch_bounds__(512) fft_tile_kernel(const C2 *in, C2 *out, TileParams p, const C2 *__restrict__ W,
-                                                        const C2 *__restrict__ Whi, const C2 *__restrict__ Wlo) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ void tile_fft_body(const C2 *in, C2 *out, const TileParams &p, const C2 *__restrict__ W, const C2 *__restrict__ Whi,
+                              const C2 *__restrict__ Wlo, int64_t blk, unsigned char *smem_raw) {
     const int L = p.L, Lp = padded_len(L);
     C2 *bufA = reinterpret_cast<C2 *>(smem_raw);
     C2 *bufB = bufA + p.C * Lp;
-    const int64_t b0 = (int64_t)blockIdx.x * p.C;
+    const int64_t b0 = blk * p.C;
     const int lines = (int)min((int64_t)p.C, p.nlines - b0);
     if (lines <= 0) return;
     const int tot = lines * L;
@@ -386,6 +387,13 @@ __global__ void __launch_bounds__(512) fft_tile_kernel(const C2 *in, C2 *out, Ti
     }
 }
 
+template <int SIGN, typename T>
+__global__ void __launch_bounds__(512) fft_tile_kernel(const C2 *in, C2 *out, TileParams p, const C2 *__restrict__ W,
+                                                        const C2 *__restrict__ Whi, const C2 *__restrict__ Wlo) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tile_fft_body<SIGN, T>(in, out, p, W, Whi, Wlo, (int64_t)blockIdx.x, smem_raw);
+}
+
 // ---------------------------------------------------------------------------
 // Table generation (FP64, sincospi), rounded to T.
 // ---------------------------------------------------------------------------
@@ -429,9 +437,8 @@ template <typename T> __global__ void d2t_kernel(C2 *out, const double2 *in, int
 // ---------------------------------------------------------------------------
 // tmp[b][i] = a[b][i] * conj(bk1[i]) (forward) or * bk1[i] (inverse), zero padded to nB.
 template <int SIGN, typename T>
-__global__ void bluestein_pre_kernel(const C2 *a, int64_t dist, C2 *tmp, const C2 *__restrict__ bk1, int64_t n, int64_t nB,
-                                     int64_t batch) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void bluestein_pre_body(const C2 *a, int64_t dist, C2 *tmp, const C2 *__restrict__ bk1, int64_t n, int64_t nB,
+                                     int64_t batch, int64_t idx) {
     if (idx >= batch * nB) return;
     int64_t b = idx / nB, i = idx - b * nB;
     C2 v = mk<T>(0, 0);
@@ -443,23 +450,38 @@ __global__ void bluestein_pre_kernel(const C2 *a, int64_t dist, C2 *tmp, const C
 }
 
 template <int SIGN, typename T>
-__global__ void bluestein_mul_kernel(C2 *tmp, const C2 *__restrict__ bk2, int64_t nB, int64_t total) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__global__ void bluestein_pre_kernel(const C2 *a, int64_t dist, C2 *tmp, const C2 *__restrict__ bk1, int64_t n, int64_t nB,
+                                     int64_t batch) {
+    bluestein_pre_body<SIGN, T>(a, dist, tmp, bk1, n, nB, batch, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
+template <int SIGN, typename T>
+__device__ __forceinline__ void bluestein_mul_body(C2 *tmp, const C2 *__restrict__ bk2, int64_t nB, int64_t total, int64_t idx) {
     if (idx >= total) return;
     C2 w = __ldg(&bk2[idx % nB]);
     tmp[idx] = SIGN < 0 ? cmul<T>(tmp[idx], w) : cmulc<T>(tmp[idx], w);
 }
 
 template <int SIGN, typename T>
-__global__ void bluestein_post_kernel(C2 *a, int64_t dist, const C2 *tmp, const C2 *__restrict__ bk1, int64_t n, int64_t nB,
-                                      int64_t batch, T scale) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__global__ void bluestein_mul_kernel(C2 *tmp, const C2 *__restrict__ bk2, int64_t nB, int64_t total) {
+    bluestein_mul_body<SIGN, T>(tmp, bk2, nB, total, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
+template <int SIGN, typename T>
+__device__ __forceinline__ void bluestein_post_body(C2 *a, int64_t dist, const C2 *tmp, const C2 *__restrict__ bk1, int64_t n, int64_t nB,
+                                      int64_t batch, T scale, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
     C2 x = tmp[b * nB + i], w = __ldg(&bk1[i]);
     C2 v = SIGN < 0 ? cmulc<T>(x, w) : cmul<T>(x, w);
     if (scale != (T)1) v = cscale<T>(v, scale);
     a[b * dist + i] = v;
+}
+
+template <int SIGN, typename T>
+__global__ void bluestein_post_kernel(C2 *a, int64_t dist, const C2 *tmp, const C2 *__restrict__ bk1, int64_t n, int64_t nB,
+                                      int64_t batch, T scale) {
+    bluestein_post_body<SIGN, T>(a, dist, tmp, bk1, n, nB, batch, scale, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -481,9 +503,8 @@ __device__ __forceinline__ void real_split(C2 zk, C2 zh, C2 w, C2 &xk) {
 
 // In place: a holds Z (h complex); writes the packed realForward layout.
 template <typename T>
-__global__ void real_post_packed_kernel(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr) {
+__device__ __forceinline__ void real_post_packed_body(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr, int64_t idx) {
     const int64_t h = n / 2, q = h / 2 + 1;  // pairs k = 0..h/2
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * q) return;
     int64_t b = idx / q, k = idx - b * q;
     C2 *z = reinterpret_cast<C2 *>(a + b * dist);
@@ -505,13 +526,17 @@ __global__ void real_post_packed_kernel(T *a, int64_t dist, int64_t n, int64_t b
     z[k] = xk;
 }
 
+template <typename T>
+__global__ void real_post_packed_kernel(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr) {
+    real_post_packed_body<T>(a, dist, n, batch, Wr, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // Out of place: z (h complex) -> full spectrum F (n complex) in out.
 // SIGN=+1 writes the e^{+} transform (z must be the e^{+} FFT), times scale.
 template <int SIGN, typename T>
-__global__ void real_post_full_kernel(const T *zin, int64_t zdist, T *out, int64_t odist, int64_t n, int64_t batch,
-                                      const C2 *__restrict__ Wr, T scale) {
+__device__ __forceinline__ void real_post_full_body(const T *zin, int64_t zdist, T *out, int64_t odist, int64_t n, int64_t batch,
+                                      const C2 *__restrict__ Wr, T scale, int64_t idx) {
     const int64_t h = n / 2, q = h / 2 + 1;
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * q) return;
     int64_t b = idx / q, k = idx - b * q;
     const C2 *z = reinterpret_cast<const C2 *>(zin + b * zdist);
@@ -540,12 +565,17 @@ __global__ void real_post_full_kernel(const T *zin, int64_t zdist, T *out, int64
     }
 }
 
+template <int SIGN, typename T>
+__global__ void real_post_full_kernel(const T *zin, int64_t zdist, T *out, int64_t odist, int64_t n, int64_t batch,
+                                      const C2 *__restrict__ Wr, T scale) {
+    real_post_full_body<SIGN, T>(zin, zdist, out, odist, n, batch, Wr, scale, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // In place: packed spectrum -> Z (h complex) whose e^{+} h-point FFT is
 // (n/2) * x interleaved; everything times `mult`.
 template <typename T>
-__global__ void real_pre_inverse_kernel(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr, T mult) {
+__device__ __forceinline__ void real_pre_inverse_body(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr, T mult, int64_t idx) {
     const int64_t h = n / 2, q = h / 2 + 1;
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * q) return;
     int64_t b = idx / q, k = idx - b * q;
     C2 *z = reinterpret_cast<C2 *>(a + b * dist);
@@ -575,20 +605,28 @@ __global__ void real_pre_inverse_kernel(T *a, int64_t dist, int64_t n, int64_t b
     z[k] = zk;
 }
 
+template <typename T>
+__global__ void real_pre_inverse_kernel(T *a, int64_t dist, int64_t n, int64_t batch, const C2 *__restrict__ Wr, T mult) {
+    real_pre_inverse_body<T>(a, dist, n, batch, Wr, mult, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // Odd-n (and general) helpers working through a full complex buffer.
 // tmp[b][i] = (a[b][i], 0)
 template <typename T>
-__global__ void real_to_complex_kernel(const T *a, int64_t dist, C2 *tmp, int64_t n, int64_t batch) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void real_to_complex_body(const T *a, int64_t dist, C2 *tmp, int64_t n, int64_t batch, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
     tmp[idx] = mk<T>(a[b * dist + i], (T)0);
 }
 
+template <typename T>
+__global__ void real_to_complex_kernel(const T *a, int64_t dist, C2 *tmp, int64_t n, int64_t batch) {
+    real_to_complex_body<T>(a, dist, tmp, n, batch, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // full spectrum F (n complex) -> packed realForward layout (fft/DoubleFFT_1D.java:433-451)
 template <typename T>
-__global__ void pack_from_full_kernel(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void pack_from_full_body(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
     const C2 *f = F + b * n;
@@ -602,10 +640,14 @@ __global__ void pack_from_full_kernel(const C2 *F, T *a, int64_t dist, int64_t n
     a[b * dist + i] = v;
 }
 
+template <typename T>
+__global__ void pack_from_full_kernel(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch) {
+    pack_from_full_body<T>(F, a, dist, n, batch, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // packed -> full Hermitian spectrum
 template <typename T>
-__global__ void unpack_to_full_kernel(const T *a, int64_t dist, C2 *F, int64_t n, int64_t batch) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void unpack_to_full_body(const T *a, int64_t dist, C2 *F, int64_t n, int64_t batch, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, k = idx - b * n;
     const T *p = a + b * dist;
@@ -619,20 +661,28 @@ __global__ void unpack_to_full_kernel(const T *a, int64_t dist, C2 *F, int64_t n
     F[idx] = v;
 }
 
+template <typename T>
+__global__ void unpack_to_full_kernel(const T *a, int64_t dist, C2 *F, int64_t n, int64_t batch) {
+    unpack_to_full_body<T>(a, dist, F, n, batch, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // a[b][i] = Re(F[b][i]) * mult
 template <typename T>
-__global__ void real_part_kernel(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch, T mult) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void real_part_body(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch, T mult, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
     a[b * dist + i] = F[idx].x * mult;
 }
 
+template <typename T>
+__global__ void real_part_kernel(const C2 *F, T *a, int64_t dist, int64_t n, int64_t batch, T mult) {
+    real_part_body<T>(F, a, dist, n, batch, mult, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // Copies batch*len complex (strided) with an optional scale and conjugation.
 template <typename T>
-__global__ void copy_complex_kernel(const C2 *src, int64_t sdist, C2 *dst, int64_t ddist, int64_t len, int64_t batch,
-                                    T scale, int conj) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void copy_complex_body(const C2 *src, int64_t sdist, C2 *dst, int64_t ddist, int64_t len, int64_t batch,
+                                    T scale, int conj, int64_t idx) {
     if (idx >= batch * len) return;
     int64_t b = idx / len, i = idx - b * len;
     C2 v = src[b * sdist + i];
@@ -641,20 +691,30 @@ __global__ void copy_complex_kernel(const C2 *src, int64_t sdist, C2 *dst, int64
     dst[b * ddist + i] = v;
 }
 
+template <typename T>
+__global__ void copy_complex_kernel(const C2 *src, int64_t sdist, C2 *dst, int64_t ddist, int64_t len, int64_t batch,
+                                    T scale, int conj) {
+    copy_complex_body<T>(src, sdist, dst, ddist, len, batch, scale, conj, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // DCT-II / DCT-III / DST / DHT passes around a real FFT of length n.
 // Wd[k] = e^{-i pi k / (2n)}, k < n.
 // ---------------------------------------------------------------------------
 // v_j = x_2j, v_{n-1-j} = x_2j+1 (DST: odd inputs negated)
 template <typename T>
-__global__ void dct2_pre_kernel(const T *a, int64_t dist, T *v, int64_t vdist, int64_t n, int64_t batch, int dst) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void dct2_pre_body(const T *a, int64_t dist, T *v, int64_t vdist, int64_t n, int64_t batch, int dst, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
     T x = a[b * dist + i];
     int64_t j = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
     if (dst && (i & 1)) x = -x;
     v[b * vdist + j] = x;
+}
+
+template <typename T>
+__global__ void dct2_pre_kernel(const T *a, int64_t dist, T *v, int64_t vdist, int64_t n, int64_t batch, int dst) {
+    dct2_pre_body<T>(a, dist, v, vdist, n, batch, dst, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
 }
 
 // reads V_k (k <= n/2 packed, conj-mirrored above)
@@ -671,9 +731,8 @@ template <typename T> __device__ __forceinline__ C2 packed_get(const T *p, int64
 
 // C_k = Re(e^{-i pi k/2n} V_k) * mult (k=0: * mult0); DST writes C_k to n-1-k.
 template <typename T>
-__global__ void dct2_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch,
-                                 const C2 *__restrict__ Wd, T mult, T mult0, int dst) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void dct2_post_body(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch,
+                                 const C2 *__restrict__ Wd, T mult, T mult0, int dst, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, k = idx - b * n;
     C2 V = packed_get<T>(v + b * vdist, n, k);
@@ -682,14 +741,19 @@ __global__ void dct2_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, 
     a[b * dist + (dst ? n - 1 - k : k)] = c;
 }
 
+template <typename T>
+__global__ void dct2_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch,
+                                 const C2 *__restrict__ Wd, T mult, T mult0, int dst) {
+    dct2_post_body<T>(v, vdist, a, dist, n, batch, Wd, mult, mult0, dst, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // DCT-III: from coefficients b_k (DST: read reversed) build the packed
 // spectrum of V_k = e^{i pi k/2n} (C_k - i C_{n-k}), C_k = g_k * b_k with
 // g_0 = mult0, g_k = mult.  Thread k <= n/2 writes V_k.
 template <typename T>
-__global__ void dct3_pre_kernel(const T *a, int64_t dist, T *v, int64_t vdist, int64_t n, int64_t batch,
-                                const C2 *__restrict__ Wd, T mult, T mult0, int dst) {
+__device__ __forceinline__ void dct3_pre_body(const T *a, int64_t dist, T *v, int64_t vdist, int64_t n, int64_t batch,
+                                const C2 *__restrict__ Wd, T mult, T mult0, int dst, int64_t idx) {
     const int64_t q = n / 2 + 1;
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= batch * q) return;
     int64_t b = idx / q, k = idx - b * q;
     const T *p = a + b * dist;
@@ -709,10 +773,15 @@ __global__ void dct3_pre_kernel(const T *a, int64_t dist, T *v, int64_t vdist, i
     else { o[2 * k] = V.x; o[2 * k + 1] = V.y; }
 }
 
+template <typename T>
+__global__ void dct3_pre_kernel(const T *a, int64_t dist, T *v, int64_t vdist, int64_t n, int64_t batch,
+                                const C2 *__restrict__ Wd, T mult, T mult0, int dst) {
+    dct3_pre_body<T>(a, dist, v, vdist, n, batch, Wd, mult, mult0, dst, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // x_2j = v_j, x_2j+1 = v_{n-1-j}; DST negates the odd outputs.
 template <typename T>
-__global__ void dct3_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, int dst) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void dct3_post_body(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, int dst, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, i = idx - b * n;
     int64_t j = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
@@ -721,14 +790,23 @@ __global__ void dct3_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, 
     a[b * dist + i] = x;
 }
 
+template <typename T>
+__global__ void dct3_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, int dst) {
+    dct3_post_body<T>(v, vdist, a, dist, n, batch, dst, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // H_k = Re X_k - Im X_k from the packed spectrum (dht/DoubleDHT_1D.java:94-159)
 template <typename T>
-__global__ void dht_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, T mult) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void dht_post_body(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, T mult, int64_t idx) {
     if (idx >= batch * n) return;
     int64_t b = idx / n, k = idx - b * n;
     C2 X = packed_get<T>(v + b * vdist, n, k);
     a[b * dist + k] = (X.x - X.y) * mult;
+}
+
+template <typename T>
+__global__ void dht_post_kernel(const T *v, int64_t vdist, T *a, int64_t dist, int64_t n, int64_t batch, T mult) {
+    dht_post_body<T>(v, vdist, a, dist, n, batch, mult, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -833,19 +911,25 @@ __global__ void transpose_kernel(const E *in, E *out, int64_t R, int64_t C, int6
     }
 }
 
-template <typename T> __global__ void scale_kernel(T *a, int64_t dist, int64_t len, int64_t batch, T s) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+template <typename T> __device__ __forceinline__ void scale_body(T *a, int64_t dist, int64_t len, int64_t batch, T s, int64_t idx) {
     if (idx >= batch * len) return;
     int64_t b = idx / len, i = idx - b * len;
     a[b * dist + i] *= (T)s;
 }
 
+template <typename T> __global__ void scale_kernel(T *a, int64_t dist, int64_t len, int64_t batch, T s) {
+    scale_body(a, dist, len, batch, s, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // a[b][i] = src[b][i] (real, strided)
-template <typename T> __global__ void copy_real_kernel(const T *src, int64_t sdist, T *dst, int64_t ddist, int64_t len, int64_t batch) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+template <typename T> __device__ __forceinline__ void copy_real_body(const T *src, int64_t sdist, T *dst, int64_t ddist, int64_t len, int64_t batch, int64_t idx) {
     if (idx >= batch * len) return;
     int64_t b = idx / len, i = idx - b * len;
     dst[b * ddist + i] = src[b * sdist + i];
+}
+
+template <typename T> __global__ void copy_real_kernel(const T *src, int64_t sdist, T *dst, int64_t ddist, int64_t len, int64_t batch) {
+    copy_real_body(src, sdist, dst, ddist, len, batch, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
 }
 
 #undef C2

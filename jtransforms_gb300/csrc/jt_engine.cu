@@ -14,6 +14,7 @@
 //             tables generated in FP64 on the device.
 #include "jt_device.cuh"
 #include "jt_stockham.cuh"
+#include "jt_batch.cuh"
 #include "../../include/jtgpu.h"
 
 #include <cuda.h>
@@ -75,7 +76,29 @@ struct Ctx {
     cudaStream_t s = nullptr;
     bool dry = false;
     Arena *ws = nullptr;
+    // batch recording: steps are appended here instead of launched, each
+    // depending on the previous step of the same transform
+    std::vector<BOp> *rec = nullptr;
+    int rec_prev = -1;
 };
+
+static void emit(Ctx &c, BOp &o) {
+    o.dep = c.rec_prev;
+    c.rec->push_back(o);
+    c.rec_prev = (int)c.rec->size() - 1;
+}
+
+template <typename T> static BOp elem_op(int kind, int sign, int64_t total) {
+    BOp o;
+    memset(&o, 0, sizeof(o));
+    o.type = BOP_ELEM;
+    o.prec = sizeof(T) == 4 ? 0 : 1;
+    o.kind = kind;
+    o.sign = sign;
+    o.total = total;
+    o.ntasks = (int)((total + JT_BATCH_ELEMS_PER_TASK - 1) / JT_BATCH_ELEMS_PER_TASK);
+    return o;
+}
 
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
@@ -296,11 +319,71 @@ template <typename T> struct Fft1 {
 
     int make_chirp();
 
+    // Batch recording of a line pass: the generic tile kernel (any layout,
+    // lengths up to the tile kernel's limit) or, for the one double
+    // power-of-two length beyond it (8192), the plain register kernel.
+    int record_lines(Ctx &ctx, const C2 *in, C2 *out, int64_t nlines, const Layout &lin, const Layout &lout, int sign,
+                     double scale, int64_t tw_n, int64_t tw_inner, const C2 *Whi_, const C2 *Wlo_, int tw_lo_bits) const {
+        BOp o;
+        memset(&o, 0, sizeof(o));
+        o.prec = sizeof(T) == 4 ? 0 : 1;
+        o.sign = sign;
+        o.in = in;
+        o.out = out;
+        o.W = W;
+        o.Whi = Whi_;
+        o.Wlo = Wlo_;
+        if (generic_ok(n)) {
+            const int L = (int)n;
+            const int Lp = padded_len(L);
+            const bool strided = lin.estride != 1 || lout.estride != 1;
+            int64_t target = sizeof(T) == 4 ? 4096 : 2048;
+            int C = (int)std::max<int64_t>(1, target / L);
+            if (strided) C = std::max(C, sizeof(T) == 4 ? 16 : 8);
+            size_t per_line = 2 * (size_t)Lp * sizeof(C2);
+            int cmax = (int)std::max<size_t>(1, (size_t)g_smem_optin / per_line);
+            C = std::min(C, cmax);
+            if ((int64_t)C > nlines) C = (int)nlines;
+            std::vector<int> rr = radix.empty() ? direct_radices(n) : radix;
+            o.type = BOP_TILE;
+            o.tp.L = L;
+            o.tp.npass = (int)rr.size();
+            for (int i = 0; i < o.tp.npass; i++) o.tp.radix[i] = rr[i];
+            o.tp.C = C;
+            o.tp.nlines = nlines;
+            o.tp.lin = lin;
+            o.tp.lout = lout;
+            o.tp.scale = scale;
+            o.tp.scalef = (float)scale;
+            o.tp.do_scale = scale != 1.0;
+            o.tp.tw_n = tw_n;
+            o.tp.tw_inner = tw_inner;
+            o.tp.tw_lo_bits = tw_lo_bits;
+            o.ntasks = (int)cdiv(nlines, C);
+            o.smem = (int)(per_line * C);
+        } else if (sizeof(T) == 8 && n == 8192 && lin.estride == 1 && lout.estride == 1 && tw_n == 0) {
+            o.type = BOP_STOCK;
+            o.sp.nlines = nlines;
+            o.sp.lin = lin;
+            o.sp.lout = lout;
+            o.sp.scale = scale;
+            o.sp.scalef = (float)scale;
+            o.sp.do_scale = scale != 1.0;
+            o.ntasks = (int)nlines;
+            o.smem = (int)Stockham<double, 8192, 0, -1>::SMEM;
+        } else {
+            return JT_EINVAL;  // no single-CTA step for this line in a batch
+        }
+        emit(ctx, o);
+        return JT_OK;
+    }
+
     // DIRECT pass over `nlines` lines with arbitrary layouts.
     int exec_direct(Ctx &ctx, const C2 *in, C2 *out, int64_t nlines, const Layout &lin, const Layout &lout, int sign,
                     double scale, int64_t tw_n = 0, int64_t tw_inner = 1, const C2 *Whi_ = nullptr, const C2 *Wlo_ = nullptr,
                     int tw_lo_bits = 0, int hint_discard_in = 0, int hint_stream_out = 1) const {
         if (nlines <= 0) return JT_OK;
+        if (ctx.rec) return record_lines(ctx, in, out, nlines, lin, lout, sign, scale, tw_n, tw_inner, Whi_, Wlo_, tw_lo_bits);
         if (reg) {
             int mode = -1;
             if (lin.estride == 1 && lout.estride == 1) mode = 0;
@@ -411,6 +494,13 @@ template <typename T> struct Fft1 {
         switch (algo) {
             case ALG_TRIVIAL: {
                 if (in == out && scale == 1.0) return JT_OK;
+                if (ctx.rec) {
+                    BOp o = elem_op<T>(EK_COPY_COMPLEX, 0, batch);
+                    o.e.p[0] = in; o.e.p[1] = out; o.e.i[0] = din; o.e.i[1] = dout; o.e.i[2] = 1; o.e.i[3] = batch;
+                    o.e.d[0] = scale; o.e.f = 0;
+                    emit(ctx, o);
+                    return JT_OK;
+                }
                 LAUNCH1D(ctx, batch, copy_complex_kernel<T>, in, din, out, dout, (int64_t)1, batch, scale, 0);
                 return JT_OK;
             }
@@ -435,13 +525,26 @@ template <typename T> struct Fft1 {
                 C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * chunk * nB, ctx.dry);
                 for (int64_t b = 0; b < batch; b += chunk) {
                     int64_t cb = std::min(chunk, batch - b);
-                    if (sign < 0) LAUNCH1D(ctx, cb * nB, (bluestein_pre_kernel<-1, T>), in + b * din, din, tmp, bk1, n, nB, cb);
+                    if (ctx.rec) {
+                        BOp o = elem_op<T>(EK_BLUE_PRE, sign, cb * nB);
+                        o.e.p[0] = in + b * din; o.e.p[1] = tmp; o.e.p[2] = bk1; o.e.i[0] = din; o.e.i[1] = n; o.e.i[2] = nB; o.e.i[3] = cb;
+                        emit(ctx, o);
+                    } else if (sign < 0) LAUNCH1D(ctx, cb * nB, (bluestein_pre_kernel<-1, T>), in + b * din, din, tmp, bk1, n, nB, cb);
                     else LAUNCH1D(ctx, cb * nB, (bluestein_pre_kernel<1, T>), in + b * din, din, tmp, bk1, n, nB, cb);
                     JT_TRY(pbl->exec(ctx, tmp, nB, tmp, nB, cb, -1, 1.0));
-                    if (sign < 0) LAUNCH1D(ctx, cb * nB, (bluestein_mul_kernel<-1, T>), tmp, bk2, nB, cb * nB);
+                    if (ctx.rec) {
+                        BOp o = elem_op<T>(EK_BLUE_MUL, sign, cb * nB);
+                        o.e.p[0] = tmp; o.e.p[1] = bk2; o.e.i[0] = nB; o.e.i[1] = cb * nB;
+                        emit(ctx, o);
+                    } else if (sign < 0) LAUNCH1D(ctx, cb * nB, (bluestein_mul_kernel<-1, T>), tmp, bk2, nB, cb * nB);
                     else LAUNCH1D(ctx, cb * nB, (bluestein_mul_kernel<1, T>), tmp, bk2, nB, cb * nB);
                     JT_TRY(pbl->exec(ctx, tmp, nB, tmp, nB, cb, 1, 1.0));
-                    if (sign < 0) LAUNCH1D(ctx, cb * n, (bluestein_post_kernel<-1, T>), out + b * dout, dout, tmp, bk1, n, nB, cb, scale);
+                    if (ctx.rec) {
+                        BOp o = elem_op<T>(EK_BLUE_POST, sign, cb * n);
+                        o.e.p[0] = out + b * dout; o.e.p[1] = tmp; o.e.p[2] = bk1; o.e.i[0] = dout; o.e.i[1] = n; o.e.i[2] = nB;
+                        o.e.i[3] = cb; o.e.d[0] = scale;
+                        emit(ctx, o);
+                    } else if (sign < 0) LAUNCH1D(ctx, cb * n, (bluestein_post_kernel<-1, T>), out + b * dout, dout, tmp, bk1, n, nB, cb, scale);
                     else LAUNCH1D(ctx, cb * n, (bluestein_post_kernel<1, T>), out + b * dout, dout, tmp, bk1, n, nB, cb, scale);
                 }
                 return JT_OK;
@@ -526,13 +629,25 @@ template <typename T> struct Real1 {
         if (n == 1 || batch <= 0) return JT_OK;
         if (even()) {
             JT_TRY(half->exec(ctx, (C2 *)a, dist / 2, (C2 *)a, dist / 2, batch, -1, 1.0));
-            LAUNCH1D(ctx, batch * (n / 4 + 1), real_post_packed_kernel<T>, a, dist, n, batch, Wr);
+            if (ctx.rec) {
+                BOp o = elem_op<T>(EK_REAL_POST_PACKED, 0, batch * (n / 4 + 1));
+                o.e.p[0] = a; o.e.p[1] = Wr; o.e.i[0] = dist; o.e.i[1] = n; o.e.i[2] = batch;
+                emit(ctx, o);
+            } else LAUNCH1D(ctx, batch * (n / 4 + 1), real_post_packed_kernel<T>, a, dist, n, batch, Wr);
             return JT_OK;
         }
         C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * n, ctx.dry);
-        LAUNCH1D(ctx, batch * n, real_to_complex_kernel<T>, a, dist, tmp, n, batch);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_R2C, 0, batch * n);
+            o.e.p[0] = a; o.e.p[1] = tmp; o.e.i[0] = dist; o.e.i[1] = n; o.e.i[2] = batch;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, real_to_complex_kernel<T>, a, dist, tmp, n, batch);
         JT_TRY(full->exec(ctx, tmp, n, tmp, n, batch, -1, 1.0));
-        LAUNCH1D(ctx, batch * n, pack_from_full_kernel<T>, tmp, a, dist, n, batch);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_PACK_FULL, 0, batch * n);
+            o.e.p[0] = tmp; o.e.p[1] = a; o.e.i[0] = dist; o.e.i[1] = n; o.e.i[2] = batch;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, pack_from_full_kernel<T>, tmp, a, dist, n, batch);
         return JT_OK;
     }
 
@@ -541,6 +656,15 @@ template <typename T> struct Real1 {
     int fwd_full(Ctx &ctx, T *a, int64_t dist, int64_t batch, int sign, double scale) const {
         if (batch <= 0) return JT_OK;
         if (n == 1) {
+            if (ctx.rec) {
+                BOp o = elem_op<T>(EK_SCALE, 0, batch);
+                o.e.p[0] = a; o.e.i[0] = dist; o.e.i[1] = 1; o.e.i[2] = batch; o.e.d[0] = scale;
+                emit(ctx, o);
+                BOp o2 = elem_op<T>(EK_SCALE, 0, batch);
+                o2.e.p[0] = a + 1; o2.e.i[0] = dist; o2.e.i[1] = 1; o2.e.i[2] = batch; o2.e.d[0] = 0.0;
+                emit(ctx, o2);
+                return JT_OK;
+            }
             LAUNCH1D(ctx, batch, scale_kernel<T>, a, dist, (int64_t)1, batch, scale);
             LAUNCH1D(ctx, batch, scale_kernel<T>, a + 1, dist, (int64_t)1, batch, 0.0);
             return JT_OK;
@@ -549,16 +673,29 @@ template <typename T> struct Real1 {
             const int64_t h = n / 2;
             C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * h, ctx.dry);
             JT_TRY(half->exec(ctx, (const C2 *)a, dist / 2, tmp, h, batch, sign, 1.0));
-            if (sign < 0)
+            if (ctx.rec) {
+                BOp o = elem_op<T>(EK_REAL_POST_FULL, sign, batch * (h / 2 + 1));
+                o.e.p[0] = tmp; o.e.p[1] = a; o.e.p[2] = Wr; o.e.i[0] = 2 * h; o.e.i[1] = dist; o.e.i[2] = n; o.e.i[3] = batch;
+                o.e.d[0] = scale;
+                emit(ctx, o);
+            } else if (sign < 0)
                 LAUNCH1D(ctx, batch * (h / 2 + 1), (real_post_full_kernel<-1, T>), (const T *)tmp, 2 * h, a, dist, n, batch, Wr, scale);
             else
                 LAUNCH1D(ctx, batch * (h / 2 + 1), (real_post_full_kernel<1, T>), (const T *)tmp, 2 * h, a, dist, n, batch, Wr, scale);
             return JT_OK;
         }
         C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * n, ctx.dry);
-        LAUNCH1D(ctx, batch * n, real_to_complex_kernel<T>, a, dist, tmp, n, batch);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_R2C, 0, batch * n);
+            o.e.p[0] = a; o.e.p[1] = tmp; o.e.i[0] = dist; o.e.i[1] = n; o.e.i[2] = batch;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, real_to_complex_kernel<T>, a, dist, tmp, n, batch);
         JT_TRY(full->exec(ctx, tmp, n, tmp, n, batch, sign, scale));
-        LAUNCH1D(ctx, batch * n, copy_complex_kernel<T>, tmp, n, (C2 *)a, dist / 2, n, batch, 1.0, 0);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_COPY_COMPLEX, 0, batch * n);
+            o.e.p[0] = tmp; o.e.p[1] = a; o.e.i[0] = n; o.e.i[1] = dist / 2; o.e.i[2] = n; o.e.i[3] = batch; o.e.d[0] = 1.0;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, copy_complex_kernel<T>, tmp, n, (C2 *)a, dist / 2, n, batch, 1.0, 0);
         return JT_OK;
     }
 
@@ -566,18 +703,36 @@ template <typename T> struct Real1 {
     int inv_packed(Ctx &ctx, T *a, int64_t dist, int64_t batch, double factor) const {
         if (batch <= 0) return JT_OK;
         if (n == 1) {
-            if (factor != 1.0) LAUNCH1D(ctx, batch, scale_kernel<T>, a, dist, (int64_t)1, batch, factor);
+            if (factor != 1.0) {
+                if (ctx.rec) {
+                    BOp o = elem_op<T>(EK_SCALE, 0, batch);
+                    o.e.p[0] = a; o.e.i[0] = dist; o.e.i[1] = 1; o.e.i[2] = batch; o.e.d[0] = factor;
+                    emit(ctx, o);
+                } else LAUNCH1D(ctx, batch, scale_kernel<T>, a, dist, (int64_t)1, batch, factor);
+            }
             return JT_OK;
         }
         if (even()) {
-            LAUNCH1D(ctx, batch * (n / 4 + 1), real_pre_inverse_kernel<T>, a, dist, n, batch, Wr, factor * 2.0 / (double)n);
+            if (ctx.rec) {
+                BOp o = elem_op<T>(EK_REAL_PRE_INV, 0, batch * (n / 4 + 1));
+                o.e.p[0] = a; o.e.p[1] = Wr; o.e.i[0] = dist; o.e.i[1] = n; o.e.i[2] = batch; o.e.d[0] = factor * 2.0 / (double)n;
+                emit(ctx, o);
+            } else LAUNCH1D(ctx, batch * (n / 4 + 1), real_pre_inverse_kernel<T>, a, dist, n, batch, Wr, factor * 2.0 / (double)n);
             JT_TRY(half->exec(ctx, (C2 *)a, dist / 2, (C2 *)a, dist / 2, batch, 1, 1.0));
             return JT_OK;
         }
         C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * batch * n, ctx.dry);
-        LAUNCH1D(ctx, batch * n, unpack_to_full_kernel<T>, a, dist, tmp, n, batch);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_UNPACK_FULL, 0, batch * n);
+            o.e.p[0] = a; o.e.p[1] = tmp; o.e.i[0] = dist; o.e.i[1] = n; o.e.i[2] = batch;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, unpack_to_full_kernel<T>, a, dist, tmp, n, batch);
         JT_TRY(full->exec(ctx, tmp, n, tmp, n, batch, 1, 1.0));
-        LAUNCH1D(ctx, batch * n, real_part_kernel<T>, tmp, a, dist, n, batch, factor / (double)n);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_REAL_PART, 0, batch * n);
+            o.e.p[0] = tmp; o.e.p[1] = a; o.e.i[0] = dist; o.e.i[1] = n; o.e.i[2] = batch; o.e.d[0] = factor / (double)n;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, real_part_kernel<T>, tmp, a, dist, n, batch, factor / (double)n);
         return JT_OK;
     }
 };
@@ -610,7 +765,11 @@ template <typename T> struct Dct1 {
         if (n == 1 || batch <= 0) return JT_OK;
         const int64_t vd = vdist();
         T *v = (T *)ctx.ws->get(sizeof(T) * batch * vd, ctx.dry);
-        LAUNCH1D(ctx, batch * n, dct2_pre_kernel<T>, a, dist, v, vd, n, batch, (int)dst);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_DCT2_PRE, 0, batch * n);
+            o.e.p[0] = a; o.e.p[1] = v; o.e.i[0] = dist; o.e.i[1] = vd; o.e.i[2] = n; o.e.i[3] = batch; o.e.f = (int)dst;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, dct2_pre_kernel<T>, a, dist, v, vd, n, batch, (int)dst);
         JT_TRY(rf->fwd_packed(ctx, v, vd, batch));
         double mult, mult0;
         if (scale) {
@@ -619,7 +778,12 @@ template <typename T> struct Dct1 {
         } else {
             mult = mult0 = is_pow2(n) ? 1.0 : 2.0;
         }
-        LAUNCH1D(ctx, batch * n, dct2_post_kernel<T>, v, vd, a, dist, n, batch, Wd, mult, mult0, (int)dst);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_DCT2_POST, 0, batch * n);
+            o.e.p[0] = v; o.e.p[1] = a; o.e.p[2] = Wd; o.e.i[0] = vd; o.e.i[1] = dist; o.e.i[2] = n; o.e.i[3] = batch;
+            o.e.d[0] = mult; o.e.d[1] = mult0; o.e.f = (int)dst;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, dct2_post_kernel<T>, v, vd, a, dist, n, batch, Wd, mult, mult0, (int)dst);
         return JT_OK;
     }
 
@@ -637,10 +801,19 @@ template <typename T> struct Dct1 {
             q = 1.0 / (double)n;
             q0 = 0.5 / (double)n;
         }
-        LAUNCH1D(ctx, batch * (n / 2 + 1), dct3_pre_kernel<T>, a, dist, v, vd, n, batch, Wd, q * (double)n / 2.0,
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_DCT3_PRE, 0, batch * (n / 2 + 1));
+            o.e.p[0] = a; o.e.p[1] = v; o.e.p[2] = Wd; o.e.i[0] = dist; o.e.i[1] = vd; o.e.i[2] = n; o.e.i[3] = batch;
+            o.e.d[0] = q * (double)n / 2.0; o.e.d[1] = q0 * (double)n; o.e.f = (int)dst;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * (n / 2 + 1), dct3_pre_kernel<T>, a, dist, v, vd, n, batch, Wd, q * (double)n / 2.0,
                  q0 * (double)n, (int)dst);
         JT_TRY(rf->inv_packed(ctx, v, vd, batch, 1.0));
-        LAUNCH1D(ctx, batch * n, dct3_post_kernel<T>, v, vd, a, dist, n, batch, (int)dst);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_DCT3_POST, 0, batch * n);
+            o.e.p[0] = v; o.e.p[1] = a; o.e.i[0] = vd; o.e.i[1] = dist; o.e.i[2] = n; o.e.i[3] = batch; o.e.f = (int)dst;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, dct3_post_kernel<T>, v, vd, a, dist, n, batch, (int)dst);
         return JT_OK;
     }
 };
@@ -661,9 +834,17 @@ template <typename T> struct Dht1 {
         if (n == 1 || batch <= 0) return JT_OK;
         const int64_t vd = (n + 1) & ~(int64_t)1;
         T *v = (T *)ctx.ws->get(sizeof(T) * batch * vd, ctx.dry);
-        LAUNCH1D(ctx, batch * n, copy_real_kernel<T>, a, dist, v, vd, n, batch);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_COPY_REAL, 0, batch * n);
+            o.e.p[0] = a; o.e.p[1] = v; o.e.i[0] = dist; o.e.i[1] = vd; o.e.i[2] = n; o.e.i[3] = batch;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, copy_real_kernel<T>, a, dist, v, vd, n, batch);
         JT_TRY(rf->fwd_packed(ctx, v, vd, batch));
-        LAUNCH1D(ctx, batch * n, dht_post_kernel<T>, v, vd, a, dist, n, batch, mult);
+        if (ctx.rec) {
+            BOp o = elem_op<T>(EK_DHT_POST, 0, batch * n);
+            o.e.p[0] = v; o.e.p[1] = a; o.e.i[0] = vd; o.e.i[1] = dist; o.e.i[2] = n; o.e.i[3] = batch; o.e.d[0] = mult;
+            emit(ctx, o);
+        } else LAUNCH1D(ctx, batch * n, dht_post_kernel<T>, v, vd, a, dist, n, batch, mult);
         return JT_OK;
     }
 };
@@ -1247,33 +1428,149 @@ int64_t jt_launch_count(int reset) {
 }  // extern "C"
 
 // ===========================================================================
-// Mixed-size batch (config "10,000 mixed 1D transforms")
+// Mixed-size batch: many 1D transforms of different plans in one launch
+// (jt_batch.cuh describes the recording and the interpreter kernel)
 // ===========================================================================
 struct jt_batch {
     std::vector<jt_plan *> plans;
     std::vector<int> ops, scales;
     std::vector<void *> ptrs;
+    // recorded steps, on the device
+    int nops = 0, ntasks = 0, smem = 0, grid = 0;
+    BOp *d_ops = nullptr;
+    BTask *d_tasks = nullptr;
+    int *d_done = nullptr;  // completed tasks per step
+    int *d_head = nullptr;  // queue head
+    char *scratch = nullptr;    // float transforms' scratch
+    char *scratch_d = nullptr;  // double transforms' scratch
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
+    ~jt_batch() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void *p : {(void *)d_ops, (void *)d_tasks, (void *)d_done, (void *)d_head, (void *)scratch, (void *)scratch_d})
+            if (p) cudaFree(p);
+    }
 };
+
+namespace {
+
+template <typename T>
+int batch_record(jt_batch *bt, std::vector<BOp> &ops, std::vector<std::vector<int>> &chains) {
+    // size each transform's scratch with a dry run, then record its steps
+    const size_t n = bt->plans.size();
+    std::vector<size_t> need(n, 0), off(n, 0);
+    size_t total = 0;
+    for (size_t i = 0; i < n; i++) {
+        jt_plan *p = bt->plans[i];
+        if (p->prec != (sizeof(T) == 4 ? JT_FLOAT32 : JT_FLOAT64)) continue;
+        PlanImpl<T> *im = (PlanImpl<T> *)p->impl;
+        JT_TRY(im->prepare(bt->ops[i]));
+        int64_t ext = im->extent(bt->ops[i]);
+        Arena ar;
+        Ctx c;
+        c.dry = true;
+        c.ws = &ar;
+        std::lock_guard<std::mutex> g(im->mu);
+        JT_TRY(im->run(c, bt->ops[i], (T *)bt->ptrs[i], 1, (ext + 1) & ~(int64_t)1, bt->scales[i] != 0));
+        need[i] = (ar.peak + 255) & ~(size_t)255;
+        off[i] = total;
+        total += need[i];
+    }
+    if (total) {
+        char *arena = nullptr;
+        JT_CU(cudaMalloc(&arena, total));
+        (sizeof(T) == 4 ? bt->scratch : bt->scratch_d) = arena;
+        for (size_t i = 0; i < n; i++) off[i] += (size_t)arena;
+    }
+    for (size_t i = 0; i < n; i++) {
+        jt_plan *p = bt->plans[i];
+        if (p->prec != (sizeof(T) == 4 ? JT_FLOAT32 : JT_FLOAT64)) continue;
+        PlanImpl<T> *im = (PlanImpl<T> *)p->impl;
+        int64_t ext = im->extent(bt->ops[i]);
+        Arena ar;
+        ar.base = (char *)off[i];
+        ar.cap = need[i];
+        Ctx c;
+        c.dry = false;
+        c.ws = &ar;
+        c.rec = &ops;
+        c.rec_prev = -1;
+        size_t first = ops.size();
+        std::lock_guard<std::mutex> g(im->mu);
+        int st = im->run(c, bt->ops[i], (T *)bt->ptrs[i], 1, (ext + 1) & ~(int64_t)1, bt->scales[i] != 0);
+        if (st != JT_OK) return st;
+        for (size_t k = first; k < ops.size(); k++) chains[i].push_back((int)k);
+    }
+    return JT_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
 int jt_batch_create(int count, jt_plan *const *plans, const int *ops, void *const *dev_ptrs, const int *scales, jt_batch **out) {
     if (!out || count < 0 || (count > 0 && (!plans || !ops || !dev_ptrs || !scales))) return JT_EINVAL;
     *out = nullptr;
-    jt_batch *b = new (std::nothrow) jt_batch();
+    JT_TRY(device_init());
+    std::unique_ptr<jt_batch> b(new (std::nothrow) jt_batch());
     if (!b) return JT_ENOMEM;
     for (int i = 0; i < count; i++) {
-        if (!plans[i] || plans[i]->nd != 1 || !dev_ptrs[i]) { delete b; return JT_EINVAL; }
-        int st = check_op(plans[i], ops[i]);
-        if (st != JT_OK) { delete b; return st; }
+        if (!plans[i] || plans[i]->nd != 1 || !dev_ptrs[i]) return JT_EINVAL;
+        JT_TRY(check_op(plans[i], ops[i]));
+        const size_t esz = plans[i]->prec == JT_FLOAT32 ? 4 : 8;
+        if (plans[i]->kind == JT_FFT && ((uintptr_t)dev_ptrs[i] % (2 * esz))) return JT_EINVAL;
         b->plans.push_back(plans[i]);
         b->ops.push_back(ops[i]);
         b->ptrs.push_back(dev_ptrs[i]);
         b->scales.push_back(scales[i]);
     }
-    *out = b;
+    std::vector<BOp> rec;
+    std::vector<std::vector<int>> chains(count);
+    JT_TRY(batch_record<float>(b.get(), rec, chains));
+    JT_TRY(batch_record<double>(b.get(), rec, chains));
+    // tasks, stage by stage: every transform's first step, then the second...
+    std::vector<BTask> tasks;
+    size_t maxlen = 0;
+    for (auto &c : chains) maxlen = std::max(maxlen, c.size());
+    int smem = 0;
+    for (size_t s = 0; s < maxlen; s++)
+        for (auto &c : chains)
+            if (s < c.size()) {
+                const BOp &o = rec[c[s]];
+                smem = std::max(smem, o.smem);
+                for (int k = 0; k < o.ntasks; k++) tasks.push_back(BTask{c[s], k});
+            }
+    b->nops = (int)rec.size();
+    b->ntasks = (int)tasks.size();
+    b->smem = smem;
+    if (b->nops) {
+        JT_CU(cudaMalloc(&b->d_ops, sizeof(BOp) * rec.size()));
+        JT_CU(cudaMemcpy(b->d_ops, rec.data(), sizeof(BOp) * rec.size(), cudaMemcpyHostToDevice));
+        JT_CU(cudaMalloc(&b->d_done, sizeof(int) * rec.size()));
+    }
+    if (b->ntasks) {
+        JT_CU(cudaMalloc(&b->d_tasks, sizeof(BTask) * tasks.size()));
+        JT_CU(cudaMemcpy(b->d_tasks, tasks.data(), sizeof(BTask) * tasks.size(), cudaMemcpyHostToDevice));
+    }
+    JT_CU(cudaMalloc(&b->d_head, sizeof(int)));
+    JT_CU(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(smem, 1)));
+    int per_sm = 0;
+    JT_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, JT_BATCH_THREADS, std::max(smem, 1)));
+    b->grid = std::max(1, per_sm) * g_sms;
+    *out = b.release();
+    return JT_OK;
+}
+
+int jt_batch_run(jt_batch *b, void *stream) {
+    if (!b) return JT_EINVAL;
+    if (!b->ntasks) return JT_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    JT_CU(cudaMemsetAsync(b->d_done, 0, sizeof(int) * b->nops, s));
+    JT_CU(cudaMemsetAsync(b->d_head, 0, sizeof(int), s));
+    batch_kernel<<<b->grid, JT_BATCH_THREADS, std::max(b->smem, 1), s>>>(b->d_ops, b->d_tasks, b->ntasks, b->d_head, b->d_done,
+                                                                          g_err_dev);
+    g_launches++;
+    JT_CU(cudaGetLastError());
     return JT_OK;
 }
 
@@ -1287,29 +1584,37 @@ int jt_batch_run_per_transform(jt_batch *b, void *stream) {
     return JT_OK;
 }
 
-int jt_batch_run(jt_batch *b, void *stream) { return jt_batch_run_per_transform(b, stream); }
-
 int jt_batch_run_graph(jt_batch *b, void *stream) {
     if (!b) return JT_EINVAL;
-    JT_TRY(device_init());
-    JT_TRY(ensure_stream());
-    cudaStream_t s = stream ? (cudaStream_t)stream : t_state.stream;
+    cudaStream_t s = (cudaStream_t)stream;
     if (!b->graph || b->graph_stream != s) {
-        // size every plan's tables and the scratch outside the capture
-        JT_TRY(jt_batch_run(b, s));
-        JT_CU(cudaStreamSynchronize(s));
-        t_state.last = s;
         if (b->graph) cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
+        cudaStream_t cap = s;
+        bool own = false;
+        if (!cap) {  // the legacy default stream cannot be captured
+            JT_CU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            own = true;
+        }
         cudaGraph_t g = nullptr;
-        JT_CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        int st = jt_batch_run(b, s);
-        cudaError_t e = cudaStreamEndCapture(s, &g);
-        if (st != JT_OK) { if (g) cudaGraphDestroy(g); return st; }
-        if (e != cudaSuccess) { g_last_cuda = (int)e; return JT_ECUDA; }
+        JT_CU(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        int st = jt_batch_run(b, cap);
+        cudaError_t e = cudaStreamEndCapture(cap, &g);
+        if (own) cudaStreamDestroy(cap);
+        if (st != JT_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) {
+            g_last_cuda = (int)e;
+            return JT_ECUDA;
+        }
         e = cudaGraphInstantiate(&b->graph, g, 0);
         cudaGraphDestroy(g);
-        if (e != cudaSuccess) { g_last_cuda = (int)e; return JT_ECUDA; }
+        if (e != cudaSuccess) {
+            g_last_cuda = (int)e;
+            return JT_ECUDA;
+        }
         b->graph_stream = s;
     }
     JT_CU(cudaGraphLaunch(b->graph, s));
@@ -1319,7 +1624,7 @@ int jt_batch_run_graph(jt_batch *b, void *stream) {
 
 int jt_batch_destroy(jt_batch *b) {
     if (!b) return JT_EINVAL;
-    if (b->graph) cudaGraphExecDestroy(b->graph);
+    cudaDeviceSynchronize();
     delete b;
     return JT_OK;
 }

@@ -173,14 +173,14 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
 // ---------------------------------------------------------------------------
 // Plain kernel (no TMA): one tile per CTA.
 // ---------------------------------------------------------------------------
+// Tile `blk` of the plain kernel, run by the calling CTA (its shared memory at
+// smem_raw, Stockham<...>::SMEM bytes).
 template <typename T, int L, int MODE, int SIGN>
-__global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
-    stockham_kernel(const typename V2<T>::t *__restrict__ in, typename V2<T>::t *__restrict__ out, StockParams p,
-                    const typename V2<T>::t *__restrict__ W, const typename V2<T>::t *__restrict__ Whi,
-                    const typename V2<T>::t *__restrict__ Wlo) {
+__device__ void stockham_body(const typename V2<T>::t *__restrict__ in, typename V2<T>::t *__restrict__ out, const StockParams &p,
+                              const typename V2<T>::t *__restrict__ W, const typename V2<T>::t *__restrict__ Whi,
+                              const typename V2<T>::t *__restrict__ Wlo, int64_t blk, unsigned char *smem_raw) {
     typedef Stockham<T, L, MODE, SIGN> S;
     typedef typename V2<T>::t C2;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     C2 *sm = reinterpret_cast<C2 *>(smem_raw);
     const int tid = threadIdx.x;
     int c, t;
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
         c = tid % S::C;
         t = tid / S::C;
     }
-    const int64_t b0 = (int64_t)blockIdx.x * S::C;
+    const int64_t b0 = blk * S::C;
     const int64_t b = b0 + c;
     const bool valid = b < p.nlines;
     C2 v[S::E];
@@ -234,6 +234,15 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
     };
     auto xi = [&](int i) { return c * S::LP + pad(i); };
     S::run_all(v, t, sm, xi, W, store);
+}
+
+template <typename T, int L, int MODE, int SIGN>
+__global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
+    stockham_kernel(const typename V2<T>::t *__restrict__ in, typename V2<T>::t *__restrict__ out, StockParams p,
+                    const typename V2<T>::t *__restrict__ W, const typename V2<T>::t *__restrict__ Whi,
+                    const typename V2<T>::t *__restrict__ Wlo) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    stockham_body<T, L, MODE, SIGN>(in, out, p, W, Whi, Wlo, (int64_t)blockIdx.x, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
