@@ -508,14 +508,13 @@ def main():
     ap.add_argument("--no-tma", action="store_true", help="use the plain (non-TMA) power-of-two kernel")
     ap.add_argument("--direct-max", type=int, default=0, help="longest float length done in one pass")
     ap.add_argument("--no-colpass", action="store_true", help="column passes on the tile-pipelined kernel")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
     args = ap.parse_args()
     global ELEMS, SIZES
     if args.small:
         ELEMS = 2 ** 25
         args.no_cpu = args.no_other = True
         args.no_e2e = True
-    else:
-        args.no_e2e = False
     if args.sizes:
         SIZES = [int(s) for s in args.sizes.split(",")]
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

@@ -228,6 +228,7 @@ template <typename T> struct Fft1 {
     int algo = ALG_TRIVIAL;
     std::vector<int> radix;
     C2 *W = nullptr;
+    C2 *Wp = nullptr;  // pass twiddle table of the register kernel (reg plans)
     int64_t n1 = 0, n2 = 0;
     std::unique_ptr<Fft1> pa, pb, pbl;
     C2 *Whi = nullptr, *Wlo = nullptr;
@@ -236,7 +237,7 @@ template <typename T> struct Fft1 {
     C2 *bk1 = nullptr, *bk2 = nullptr;
 
     ~Fft1() {
-        for (void *p : {(void *)W, (void *)Whi, (void *)Wlo, (void *)bk1, (void *)bk2})
+        for (void *p : {(void *)W, (void *)Wp, (void *)Whi, (void *)Wlo, (void *)bk1, (void *)bk2})
             if (p) cudaFree(p);
     }
 
@@ -261,6 +262,24 @@ template <typename T> struct Fft1 {
         return JT_OK;
     }
 
+    static int make_pass_table(C2 **out, int L) {
+        const int count = stock_tw_count(L);
+        JT_CU(cudaMalloc(out, sizeof(C2) * std::max(count, 1)));
+        if (count > 0) {
+            passtw_kernel<T><<<(unsigned)cdiv(count, 256), 256>>>(*out, L);
+            g_launches++;
+            JT_CU(cudaGetLastError());
+        }
+        return JT_OK;
+    }
+    // register kernel plans need the pass table; sub-plans that fall back to
+    // the generic kernel drop it
+    int set_reg(bool on) {
+        reg = on;
+        if (reg && !Wp) return make_pass_table(&Wp, (int)n);
+        return JT_OK;
+    }
+
     static int create(int64_t n, std::unique_ptr<Fft1> &out) {
         std::unique_ptr<Fft1> f(new (std::nothrow) Fft1());
         if (!f) return JT_ENOMEM;
@@ -269,7 +288,7 @@ template <typename T> struct Fft1 {
             f->algo = ALG_TRIVIAL;
         } else if (direct_ok(n) && (!is_pow2(n) || n <= one_pass_max())) {
             f->algo = ALG_DIRECT;
-            f->reg = reg_ok(n);
+            JT_TRY(f->set_reg(reg_ok(n)));
             if (!f->reg) f->radix = direct_radices(n);
             JT_TRY(make_roots(&f->W, n, 1, n));
         } else {
@@ -362,7 +381,9 @@ template <typename T> struct Fft1 {
             o.ntasks = (int)cdiv(nlines, C);
             o.smem = (int)(per_line * C);
         } else if (sizeof(T) == 8 && n == 8192 && lin.estride == 1 && lout.estride == 1 && tw_n == 0) {
+            if (!Wp) return JT_EINVAL;
             o.type = BOP_STOCK;
+            o.W = Wp;  // the register kernel reads the pass table
             o.sp.nlines = nlines;
             o.sp.lin = lin;
             o.sp.lout = lout;
@@ -389,7 +410,7 @@ template <typename T> struct Fft1 {
             if (lin.estride == 1 && lout.estride == 1) mode = 0;
             else if (lin.estride != 1 && lout.estride != 1 && n <= 4096) mode = 1;
             else if (lin.estride == 1 && lout.estride != 1 && n <= 4096) mode = 2;
-            if (mode < 0) return JT_EINVAL;
+            if (mode < 0 || (mode == 0 && tw_n != 0)) return JT_EINVAL;  // the four-step twiddle rides on column passes
             StockParams sp;
             memset(&sp, 0, sizeof(sp));
             sp.nlines = nlines;
@@ -423,7 +444,7 @@ template <typename T> struct Fft1 {
                         ok = ok && ((uintptr_t)in % 16) == 0 && (lin.outer * esz) % 16 == 0 &&
                              (lin.inner == 1 || (lin.istride * esz) % 16 == 0) && (n * esz) % 16 == 0;
                     }
-                    if (ok && colpass_launch((int)n, mode, sign, in, sp, tin, tout, W, Whi_, Wlo_, g_err_dev, ctx.s)) {
+                    if (ok && colpass_launch((int)n, mode, sign, in, sp, tin, tout, Wp, Whi_, Wlo_, g_err_dev, ctx.s)) {
                         g_launches++;
                         return JT_OK;
                     }
@@ -444,7 +465,7 @@ template <typename T> struct Fft1 {
                 pipe = contig || ((lin.outer * esz) % 16 == 0 && (lin.inner == 1 || (lin.istride * esz) % 16 == 0));
                 pipe = pipe && (n * esz) % 16 == 0;
             }
-            if (!stockham_launch((int)n, mode, sign, in, out, sp, pipe ? &tm : nullptr, W, Whi_, Wlo_, g_err_dev, g_sms,
+            if (!stockham_launch((int)n, mode, sign, in, out, sp, pipe ? &tm : nullptr, Wp, Whi_, Wlo_, g_err_dev, g_sms,
                                  ctx.s))
                 return JT_EINVAL;
             g_launches++;

@@ -61,6 +61,65 @@ template <typename T> struct StockCfg {
     static constexpr int C(int L, int mode) { return mode == 0 ? rows_C(L) : cols_C(L); }
 };
 
+// Pass twiddle table of a length-L line (one per length, built by
+// passtw_kernel): pass P >= 1 of radix R after NS = 16^P owns NS * R entries,
+// row jm holding w_{NS R}^{jm k} for k = 0..R-1, so the R - 1 factors a
+// butterfly needs are one contiguous, 16-byte aligned run.  Passes are
+// radix 16 (E = 16 elements per thread) with a last pass of the remaining
+// radix.
+__host__ __device__ inline int stock_tw_count(int L) {
+    const int E = L >= 16 ? 16 : L;
+    int logl = 0, loge = 0;
+    while ((1 << logl) < L) logl++;
+    while ((1 << loge) < E) loge++;
+    const int nfull = loge ? logl / loge : 0, rem = loge ? 1 << (logl % loge) : 1;
+    const int npass = nfull + (rem > 1 ? 1 : 0);
+    int tot = 0, ns = 1;
+    for (int P = 0; P < npass; P++) {
+        const int R = P < nfull ? E : rem;
+        if (P >= 1) tot += ns * R;
+        ns *= R;
+    }
+    return tot;
+}
+
+template <typename T> __global__ void passtw_kernel(typename V2<T>::t *out, int L) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int E = L >= 16 ? 16 : L;
+    int logl = 0, loge = 0;
+    while ((1 << logl) < L) logl++;
+    while ((1 << loge) < E) loge++;
+    const int nfull = loge ? logl / loge : 0, rem = loge ? 1 << (logl % loge) : 1;
+    const int npass = nfull + (rem > 1 ? 1 : 0);
+    int off = 0, ns = 1;
+    for (int P = 0; P < npass; P++) {
+        const int R = P < nfull ? E : rem;
+        if (P >= 1) {
+            if (idx < off + ns * R) {
+                const int r = idx - off, jm = r / R, k = r - jm * R;
+                const int64_t den = (int64_t)ns * R;
+                const int64_t num = ((int64_t)jm * k) % den;
+                double s, c;
+                sincospi(-2.0 * (double)num / (double)den, &s, &c);
+                out[idx] = mk<T>((T)c, (T)s);
+                return;
+            }
+            off += ns * R;
+        }
+        ns *= R;
+    }
+}
+
+// Exchange slot of element i of a line whose padded copy starts at `base`.
+// The passes recognise this index type and address their strided shared-
+// memory runs as one base plus compile-time offsets.
+struct PadIdx {
+    int base;
+    __device__ __forceinline__ int operator()(int i) const { return base + pad(i); }
+};
+template <typename X> struct is_pad_idx { static constexpr bool value = false; };
+template <> struct is_pad_idx<PadIdx> { static constexpr bool value = true; };
+
 template <int R, int SIGN, typename T> __device__ __forceinline__ void dft_pow2(typename V2<T>::t *u) {
     if (R == 2) dft2<SIGN, T>(u);
     else if (R == 4) dft4v<SIGN, T>(u);
@@ -103,14 +162,33 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     template <int P> struct Tw {
         static constexpr int N = Pass<P>::NS > 1 ? Pass<P>::NB * (Pass<P>::R - 1) : 1;
     };
+    // offset of pass P's rows in the pass twiddle table (stock_tw_count)
+    template <int P> static constexpr int twoff() {
+        if constexpr (P <= 1) return 0;
+        else return twoff<P - 1>() + Pass<P - 1>::NS * Pass<P - 1>::R;
+    }
+    // W: the pass twiddle table of length L.  Float rows are read two
+    // factors per 16-byte load.
     template <int P> static __device__ __forceinline__ void load_tw(int t, const C2 *__restrict__ W, C2 (&tw)[Tw<P>::N]) {
         typedef Pass<P> PP;
         if constexpr (PP::NS > 1) {
 #pragma unroll
             for (int q = 0; q < PP::NB; q++) {
                 const int jm = (t + q * TL) & (PP::NS - 1);
+                const C2 *row = W + twoff<P>() + jm * PP::R;
+                if constexpr (sizeof(T) == 4) {
+                    // factor 1 alone, then factors (2,3), (4,5), ... in pairs
+                    tw[q * (PP::R - 1)] = __ldg(row + 1);
 #pragma unroll
-                for (int k = 1; k < PP::R; k++) tw[q * (PP::R - 1) + k - 1] = __ldg(&W[(jm * k) << PP::SHIFT]);
+                    for (int k2 = 2; k2 < PP::R; k2 += 2) {
+                        const float4 x = __ldg(reinterpret_cast<const float4 *>(row + k2));
+                        tw[q * (PP::R - 1) + k2 - 1] = make_float2(x.x, x.y);
+                        tw[q * (PP::R - 1) + k2] = make_float2(x.z, x.w);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 1; k < PP::R; k++) tw[q * (PP::R - 1) + k - 1] = __ldg(row + k);
+                }
             }
         }
     }
@@ -139,18 +217,35 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
             }
             dft_pow2<PP::R, SIGN, T>(u);
             const int idxD = (j - jm) * PP::R + jm;
+            if constexpr (!PP::LAST && is_pad_idx<XIdx>::value && (PP::NS % 16 == 0 || (PP::NS == 1 && PP::R == 16))) {
+                // pad(idxD + k NS) = pad(idxD) + k (NS + NS/16) for NS a multiple
+                // of 16; for NS = 1, R = 16: pad(16 j + k) = pad(16 j) + k
+                const int pb = xi(idxD);
+                constexpr int ST = PP::NS == 1 ? 1 : PP::NS + PP::NS / 16;
 #pragma unroll
-            for (int k = 0; k < PP::R; k++) {
-                if (PP::LAST) store(idxD + k * PP::NS, u[k], q * PP::R + k);
-                else xs[xi(idxD + k * PP::NS)] = u[k];
+                for (int k = 0; k < PP::R; k++) xs[pb + k * ST] = u[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < PP::R; k++) {
+                    if (PP::LAST) store(idxD + k * PP::NS, u[k], q * PP::R + k);
+                    else xs[xi(idxD + k * PP::NS)] = u[k];
+                }
             }
         }
         if constexpr (!PP::LAST) {
+            // the next pass's twiddles load during the exchange
             C2 tw2[Tw<P + 1>::N];
             load_tw<P + 1>(t, W, tw2);
             sync();
+            if constexpr (is_pad_idx<XIdx>::value && TL % 16 == 0) {
+                // pad(t + m TL) = pad(t) + m (TL + TL/16)
+                const int pr = xi(t);
 #pragma unroll
-            for (int m = 0; m < E; m++) v[m] = xs[xi(t + m * TL)];
+                for (int m = 0; m < E; m++) v[m] = xs[pr + m * (TL + TL / 16)];
+            } else {
+#pragma unroll
+                for (int m = 0; m < E; m++) v[m] = xs[xi(t + m * TL)];
+            }
             sync();
             run<P + 1>(v, tw2, t, xs, xi, W, store, sync);
         }
@@ -232,7 +327,7 @@ __device__ void stockham_body(const typename V2<T>::t *__restrict__ in, typename
         if (do_scale) val = cscale<T>(val, sc);
         if (valid) dst[(int64_t)pos * oes32] = val;
     };
-    auto xi = [&](int i) { return c * S::LP + pad(i); };
+    PadIdx xi{c * S::LP};
     S::run_all(v, t, sm, xi, W, store);
 }
 
@@ -313,11 +408,14 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
     int64_t tile = blockIdx.x;
     if (tid == 0 && tile < ntiles) issue(tile, stage0, &bar[0]);
 
-    const bool tw = p.tw_n != 0;
+    // the four-step twiddle belongs to the column pass (the launcher never
+    // asks the row mode for one)
+    const bool tw = MODE != 0 && p.tw_n != 0;
     const int lo_mask = (1 << p.tw_lo_bits) - 1;
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
     const int oes32 = MODE == 0 ? 1 : (int)p.lout.estride;
+    const uint64_t spol = p.stream_out ? pol : policy_evict_normal();  // output stores
     uint32_t it = 0;
     bool ok = true;
     for (; tile < ntiles; tile += gridDim.x, ++it) {
@@ -351,7 +449,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             for (int m = 0; m < S::E; m++) v[m] = st[c * L + t + m * S::TL];
         }
         __syncthreads();  // every pass-0 read is done before the exchange writes
-        auto xi = [&](int i) { return c * S::LP + pad(i); };
+        PadIdx xi{c * S::LP};
         if (MODE == 2) {
             // last pass to shared memory, then a column-coalesced store: the
             // thread's column cc is fixed, positions advance by NT / C
@@ -366,8 +464,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
                 for (int pos = tid / S::C; pos < L; pos += S::NT / S::C) {
                     C2 val = srow[pad(pos)];
                     if (do_scale) val = cscale<T>(val, sc);
-                    if (p.stream_out) __stcs(&o[(int64_t)pos * oes32], val);
-                    else o[(int64_t)pos * oes32] = val;
+                    st_hint(&o[(int64_t)pos * oes32], val, spol);
                 }
             }
         } else {
@@ -385,6 +482,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
                     if (slot == 0) {
                         const int g = S::TL * j2;
                         C2 base = twv(t * j2);
+                        if (do_scale) base = cscale<T>(base, sc);  // the scale rides on the twiddle
                         bl[0] = base;
                         bl[1] = cmul<T>(base, twv(g));
                         bl[2] = cmul<T>(base, twv(2 * g));
@@ -398,11 +496,8 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
                     C2 w = m < 4 ? bl[m & 3] : cmul<T>(bl[m & 3], gh[m >> 2]);
                     val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
                 }
-                if (do_scale) val = cscale<T>(val, sc);
-                if (valid) {
-                    if (p.stream_out) __stcs(&dst[(int64_t)pos * oes32], val);
-                    else dst[(int64_t)pos * oes32] = val;
-                }
+                if (do_scale && !tw) val = cscale<T>(val, sc);
+                if (valid) st_hint(&dst[(int64_t)pos * oes32], val, spol);
             };
             S::run_all(v, t, st, xi, W, store);
         }
@@ -440,6 +535,20 @@ template <typename T, int L> struct StockLaunch {
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stockham_pipe_kernel<T, L, MODE, SIGN>, S::NT,
                                                               S::PIPE_SMEM);
                 if (per_sm < 1) per_sm = 1;
+                // shared memory for exactly the resident blocks; the rest of
+                // the SM's 256 KB stays L1, which holds the twiddle tables
+                const int need = per_sm * ((int)S::PIPE_SMEM + 1024);
+                const int pct = (need * 100 + 228 * 1024 - 1) / (228 * 1024);
+                if (pct < 100) {
+                    cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         pct);
+                    int again = 0;
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&again, stockham_pipe_kernel<T, L, MODE, SIGN>, S::NT,
+                                                                  S::PIPE_SMEM);
+                    if (again < per_sm)
+                        cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>,
+                                             cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+                }
             }
             int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * per_sm);
             stockham_pipe_kernel<T, L, MODE, SIGN>

@@ -119,6 +119,21 @@ __device__ __forceinline__ void tensor3d_g2s_hint(void *dst, const CUtensorMap *
         : "memory");
 }
 
+__device__ __forceinline__ uint64_t policy_evict_normal() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// Global stores carrying an L2 eviction policy (evict_first for outputs that
+// are not re-read soon, evict_normal otherwise): one instruction either way.
+__device__ __forceinline__ void st_hint(float2 *p, float2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint(double2 *p, double2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(pol) : "memory");
+}
+
 // Drops a 128-byte L2 line without writing it back (its data is dead).
 __device__ __forceinline__ void discard_l2_line(const void *p) {
     asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
