@@ -201,6 +201,21 @@ def timed_calls(fn_list, restore, flush, steps, warmup, stream):
     return [[a.elapsed_time(b) for a, b in t] for t in times]
 
 
+def sixty_db(n, gen):
+    """Input set (b), 60 dB dynamic range: 8 unit-amplitude complex
+    exponentials at random bins (random phases) plus 1e-3 N(0,1), as
+    interleaved complex64 on the device."""
+    import torch
+    j = torch.arange(n, device="cuda", dtype=torch.int64)
+    bins = torch.randint(0, n, (8,), device="cuda", generator=gen)
+    ph = torch.rand(8, device="cuda", dtype=torch.float64, generator=gen) * 2 * math.pi
+    ang = 2 * math.pi * ((j[:, None] * bins[None, :]) % n).double() / n + ph[None, :]
+    z = torch.polar(torch.ones_like(ang), ang).sum(1)
+    z = z + 1e-3 * torch.complex(torch.randn(n, device="cuda", dtype=torch.float64, generator=gen),
+                                 torch.randn(n, device="cuda", dtype=torch.float64, generator=gen))
+    return torch.view_as_real(z.to(torch.complex64)).reshape(-1).contiguous()
+
+
 def blob_image(size, rng):
     """Sum of 20 Gaussian blobs (centres U[0,size)^2, sigma U[5,50] px,
     amplitude U[0,1]) plus N(0, 0.01^2) noise."""
@@ -429,15 +444,38 @@ def run_ours(args, world, rank, local):
                                            "algorithm": ["direct", "two-pass", "bluestein", "trivial"][plans[i].plan.algorithm(0)]}
                 for i, (n, ms) in enumerate(zip(SIZES, per_size_ms))}
 
-    # error of the FP32 path against FP64 (input set (a), one transform per size)
-    err = {}
-    for i, n in enumerate(SIZES):
-        x = pristine[i][: 2 * n].double()
+    # error against FP64 of one transform per size: input set (a) = the timed
+    # data, set (b) = 60 dB dynamic range
+    def rel_err(plan, xin):
+        x = xin.double()
         ref = torch.fft.fft(torch.complex(x[0::2], x[1::2]))
-        w = pristine[i][: 2 * n].clone()
-        plans[i].plan.execute(N.COMPLEX_FORWARD, w, 0, False)
+        w = xin.clone()
+        plan.execute(N.COMPLEX_FORWARD, w, 0, False)
         got = torch.complex(w[0::2].double(), w[1::2].double())
-        err[f"2^{int(math.log2(n))}"] = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        return float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+
+    err, err_b, set_b = {}, {}, []
+    for i, n in enumerate(SIZES):
+        set_b.append(sixty_db(n, g))
+        err[f"2^{int(math.log2(n))}"] = rel_err(plans[i].plan, pristine[i][: 2 * n])
+        err_b[f"2^{int(math.log2(n))}"] = rel_err(plans[i].plan, set_b[i])
+
+    # split-operand tensor-core mode beside plain FP32 (row lengths 16..2048)
+    tc = {}
+    for i, n in enumerate(SIZES):
+        if n > 2048:
+            continue
+        plans[i].plan.set_mode(N.MODE_TC_SPLIT)
+        tt = timed_calls([fns[i]], lambda _, i=i: work[i].copy_(pristine[i]), flush, max(args.steps, 3), 2, stream)[0]
+        ms = statistics.median(tt)
+        tc[f"2^{int(math.log2(n))}"] = {
+            "ms": ms, "GB/s": 2 * 8 * ELEMS / (ms * 1e-3) / 1e9, "GFLOP/s": flops_c2c(n, ELEMS // n) / (ms * 1e-3) / 1e9,
+            "plain_ms": per_size_ms[i], "rel_l2_vs_fp64_a": rel_err(plans[i].plan, pristine[i][: 2 * n]),
+            "rel_l2_vs_fp64_b": rel_err(plans[i].plan, set_b[i]),
+            "plain_rel_l2_vs_fp64_a": err[f"2^{int(math.log2(n))}"],
+            "plain_rel_l2_vs_fp64_b": err_b[f"2^{int(math.log2(n))}"]}
+        plans[i].plan.set_mode(N.MODE_FP32)
+    del set_b
 
     # end to end through the C ABI with pinned host buffers
     e2e_val = None
@@ -468,7 +506,12 @@ def run_ours(args, world, rank, local):
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
                          "kernel": "fft_tile_kernel (all launches of one 1 GiB batch call)",
                          "algorithmic_bytes_per_call": 2 * 8 * ELEMS},
-            "per_size": per_size, "rel_l2_vs_fp64": err,
+            "per_size": per_size, "rel_l2_vs_fp64": err, "rel_l2_vs_fp64_set_b": err_b,
+            "tc_split": {"per_size": tc,
+                         "scheme": "radix-16 stages as M128 N32 tcgen05 kind::tf32 products, TF32 head + FP32 remainder, "
+                                   "3 products hi*hi + lo*hi + hi*lo, FP32 accumulate in tensor memory; twiddles and "
+                                   "the last short radix on CUDA cores",
+                         "applies_to": "row passes of length 16..2048 (direct sizes); longer lengths run plain passes"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * ELEMS * len(SIZES),
                     "d2h_bytes_per_step": 8 * ELEMS * len(SIZES),
                     "path": "FloatFFT_1D plan -> jt_execute_batch on pinned host arrays"},

@@ -80,6 +80,9 @@ struct Ctx {
     // depending on the previous step of the same transform
     std::vector<BOp> *rec = nullptr;
     int rec_prev = -1;
+    // JT_MODE_TC_SPLIT: Float32 row passes of length 16..2048 run their
+    // radix-16 stages on the tensor cores (jt_tcsplit.cuh)
+    bool tc = false;
 };
 
 static void emit(Ctx &c, BOp &o) {
@@ -168,6 +171,9 @@ bool colpass_cfg(int L, int mode, int *C, int *swb, const float *);
 bool colpass_cfg(int L, int mode, int *C, int *swb, const double *);
 bool colpass_launch(int L, int mode, int sign, const float2 *in, const StockParams &p, const CUtensorMap &tin,
                     const CUtensorMap &tout, const float2 *W, const float2 *Whi, const float2 *Wlo, int *err, cudaStream_t s);
+bool tc_split_ok(int L);
+bool tc_split_launch(int L, int sign, const float2 *in, float2 *out, const StockParams &p, const float2 *W, int *err, int sms,
+                     cudaStream_t s);
 bool colpass_launch(int L, int mode, int sign, const double2 *in, const StockParams &p, const CUtensorMap &tin,
                     const CUtensorMap &tout, const double2 *W, const double2 *Whi, const double2 *Wlo, int *err, cudaStream_t s);
 
@@ -426,6 +432,16 @@ template <typename T> struct Fft1 {
             sp.stream_out = hint_stream_out;
             if (ctx.dry) return JT_OK;
             const int esz = (int)sizeof(C2);
+            // split-operand tensor-core kernel for Float32 row passes
+            if constexpr (sizeof(T) == 4) {
+                if (ctx.tc && mode == 0 && tc_split_ok((int)n)) {
+                    if (!tc_split_launch((int)n, sign, (const float2 *)in, (float2 *)out, sp, (const float2 *)Wp, g_err_dev,
+                                         g_sms, ctx.s))
+                        return JT_ECUDA;
+                    g_launches++;
+                    return JT_OK;
+                }
+            }
             // column passes: group-per-line kernel with TMA tensor load/store
             if ((mode == 1 || mode == 2) && g_opt_tma.load() && g_opt_colpass.load()) {
                 int Cc = 0, swb = 0;
@@ -1187,6 +1203,7 @@ int run_device(jt_plan *p, int op, T *a, int64_t batch, int64_t dist, bool scale
     JT_TRY(im->prepare(op));
     Ctx c;
     c.s = s;
+    c.tc = p->mode == JT_MODE_TC_SPLIT;
     c.ws = &t_state.arena;
     c.dry = true;
     t_state.arena.used = 0;
@@ -1243,6 +1260,7 @@ int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t 
     // size: array + scratch (dry run)
     Ctx c;
     c.s = s;
+    c.tc = p->mode == JT_MODE_TC_SPLIT;
     c.ws = &t_state.arena;
     c.dry = true;
     t_state.arena.used = 0;
@@ -1350,7 +1368,7 @@ int jt_plan_extent(const jt_plan *p, int op, int64_t *out_len) {
 
 int jt_plan_set_mode(jt_plan *p, int mode) {
     if (!p) return JT_EINVAL;
-    if (mode == JT_MODE_FP32) {
+    if (mode == JT_MODE_FP32 || (mode == JT_MODE_TC_SPLIT && p->prec == JT_FLOAT32)) {
         p->mode = mode;
         return JT_OK;
     }
