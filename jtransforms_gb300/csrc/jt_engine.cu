@@ -1593,6 +1593,7 @@ int jt_batch_create(int count, jt_plan *const *plans, const int *ops, void *cons
     }
     JT_CU(cudaMalloc(&b->d_head, sizeof(int)));
     JT_CU(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(smem, 1)));
+    JT_CU(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 0;
     JT_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, JT_BATCH_THREADS, std::max(smem, 1)));
     b->grid = std::max(1, per_sm) * g_sms;

@@ -34,7 +34,19 @@ template <int L> struct TcLaunch {
         static int per_sm = 0;
         if (!per_sm) {
             cudaFuncSetAttribute(tcfft_kernel<L, SIGN>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM);
+            // shared memory for the resident blocks (the occupancy query
+            // follows the carveout preference)
+            cudaFuncSetAttribute(tcfft_kernel<L, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tcfft_kernel<L, SIGN>, K::NT, K::SMEM);
+            // the register and shared-memory limits directly (the occupancy
+            // query may not count a tensor-memory kernel's blocks)
+            cudaFuncAttributes fa;
+            if (cudaFuncGetAttributes(&fa, tcfft_kernel<L, SIGN>) == cudaSuccess && fa.numRegs > 0) {
+                const int regs = (fa.numRegs + 7) / 8 * 8;
+                const int by_regs = 65536 / (regs * K::NT);
+                const int by_smem = (228 * 1024) / (K::SMEM + 1024);
+                per_sm = std::max(per_sm, std::min(by_regs, by_smem));
+            }
             if (per_sm < 1) per_sm = 1;
             if (per_sm > 8) per_sm = 8;  // 8 x 32 tensor-memory columns: half the SM's 512
         }
