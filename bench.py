@@ -34,6 +34,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SIZES = [2 ** 10, 2 ** 14, 2 ** 18, 2 ** 20, 2 ** 24]
+HEADLINE_SIZES = list(SIZES)
+# DRAM bytes (read + write) of one headline step, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum, L2 kept between launches) of
+# the 256 MiB-per-size case, scaled by 4 (traffic grows with the transforms
+# processed): 2142 + 2205 + 2178 + 2250 + 3065 MB for 2^10 .. 2^24
+TRAFFIC_PER_STEP = 11.84e9
 ELEMS = 2 ** 27          # complex elements per size per rank (1 GiB complex64)
 SEED = 20110602
 METRIC = "GFLOP/s (5N log2N) & % HBM roofline; TC-split vs plain FP32 at same error"
@@ -55,7 +61,8 @@ def flops_c2c(n, batch):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms, each line
+    time-stamped on arrival; summary() keeps the samples inside a window."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -69,7 +76,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -79,7 +86,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def __exit__(self, *a):
         if self.proc:
@@ -89,10 +96,19 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
-    def summary(self):
+    def summary(self, t0=None, t1=None):
+        """Median SM clock and the throttle reasons seen in [t0, t1], plus the
+        last sample before t0 and the first after t1 (the clock state that
+        the window starts and ends in)."""
+        rows = list(self.lines)
+        if t0 is not None:
+            inside = [r for r in rows if t0 <= r[0] <= t1]
+            before = [r for r in rows if r[0] < t0][-1:]
+            after = [r for r in rows if r[0] > t1][:1]
+            rows = before + inside + after
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in rows:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -415,6 +431,7 @@ def run_ours(args, world, rank, local):
     fns = [(lambda i=i: plans[i].plan.execute(N.COMPLEX_FORWARD, work[i], 0, False,
                                               batch=ELEMS // SIZES[i], dist=2 * SIZES[i]))
            for i in range(len(SIZES))]
+    clk = ClockSampler(local).__enter__()  # running before the warm-up: samples cover the timed region
     # warm-up (tables, scratch, clocks)
     timed_calls(fns, lambda i: work[i].copy_(pristine[i]), flush, 0, args.warmup, stream)
     if world > 1:
@@ -423,11 +440,13 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     J.launch_count(reset=True)
     t_wall0 = time.perf_counter()
-    with ClockSampler(local) as clk:
-        times = timed_calls(fns, lambda i: work[i].copy_(pristine[i]), flush, args.steps, 0, stream)
+    times = timed_calls(fns, lambda i: work[i].copy_(pristine[i]), flush, args.steps, 0, stream)
     torch.cuda.synchronize()
     launches = J.launch_count(reset=True)
-    wall = time.perf_counter() - t_wall0
+    t_wall1 = time.perf_counter()
+    wall = t_wall1 - t_wall0
+    time.sleep(0.1)  # the sample after the window
+    clk.__exit__(None, None, None)
     per_size_ms = [sum(t) / len(t) for t in times]
     step_ms = sum(per_size_ms)
     if world > 1:
@@ -503,9 +522,14 @@ def run_ours(args, world, rank, local):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded N(0,1) complex64)",
             "config": headline_config(args),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
-                         "kernel": "fft_tile_kernel (all launches of one 1 GiB batch call)",
-                         "algorithmic_bytes_per_call": 2 * 8 * ELEMS},
+                         "frac": achieved / peak,
+                         "traffic": TRAFFIC_PER_STEP * (ELEMS / 2 ** 27) if SIZES == HEADLINE_SIZES else None,
+                         "traffic_unit": "bytes per step (DRAM read + write of the five calls)",
+                         "peak_source": peak_src,
+                         "kernel": "stockham_pipe_kernel (every launch of the five 1 GiB calls: one pass at 2^10, "
+                                   "passes A and B at 2^14..2^24)",
+                         "algorithmic_bytes_per_call": 2 * 8 * ELEMS,
+                         "algorithmic_bytes_per_step": bytes_step},
             "per_size": per_size, "rel_l2_vs_fp64": err, "rel_l2_vs_fp64_set_b": err_b,
             "tc_split": {"per_size": tc,
                          "scheme": "radix-16 stages as M128 N32 tcgen05 kind::tf32 products, TF32 head + FP32 remainder, "
@@ -517,7 +541,7 @@ def run_ours(args, world, rank, local):
                     "path": "FloatFFT_1D plan -> jt_execute_batch on pinned host arrays"},
             "gpu_launches": launches,
             "timed_wall_s": wall}
-    clocks = clk.summary()
+    clocks = clk.summary(t_wall0, t_wall1)
     line["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_cpu:
         v, th, desc = cpu_sample(3.0)
