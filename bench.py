@@ -409,6 +409,8 @@ def run_ours(args, world, rank, local):
         N.set_option(N.OPT_DIRECT_MAX_F32, args.direct_max)
     if args.no_colpass:
         N.set_option(N.OPT_COLUMN_KERNEL, 0)
+    if args.chunk_mb:
+        N.set_option(N.OPT_TWOPASS_CHUNK_MB, args.chunk_mb)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -575,6 +577,7 @@ def main():
     ap.add_argument("--no-tma", action="store_true", help="use the plain (non-TMA) power-of-two kernel")
     ap.add_argument("--direct-max", type=int, default=0, help="longest float length done in one pass")
     ap.add_argument("--no-colpass", action="store_true", help="column passes on the tile-pipelined kernel")
+    ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 48)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
     args = ap.parse_args()
     global ELEMS, SIZES

@@ -154,6 +154,8 @@ int jt_batch_destroy(jt_batch *batch);
 #define JT_OPT_DIRECT_MAX_F64 2 /* the same for double (default 8192) */
 #define JT_OPT_COLUMN_KERNEL 3  /* 0 (default): column passes use the tile-pipelined kernel; 1: the
                                    line-group kernel with swizzled TMA tensor loads and stores */
+#define JT_OPT_TWOPASS_CHUNK_MB 4 /* MiB of transforms per two-pass chunk (default 48, 1..1024): the
+                                     column pass's output stays in L2 for the row pass */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 

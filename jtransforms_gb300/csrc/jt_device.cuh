@@ -840,6 +840,56 @@ __global__ void rdft2d_kernel(T *a, int64_t dist, int64_t rows, int64_t cols, in
     }
 }
 
+// rdft3d_sub (fft/DoubleFFT_3D.java:6909-7021): the packed columns 0/1 of
+// mirror (slice, row) pairs.  One thread per pair (x, y), enumerated as
+// (ii < slices/2, kk < rows/2, w in {0,1}); ii = kk = 0 has no pair.  The
+// pairs are disjoint, so any order gives the reference's result.
+template <typename T>
+__global__ void rdft3d_kernel(T *a, int64_t dist, int64_t slices, int64_t rows, int64_t cols, int64_t batch, int isgn) {
+    const int64_t n1h = slices >> 1, n2h = rows >> 1, ss = rows * cols, rs = cols;
+    const int64_t per = n1h * n2h * 2;
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= batch * per) return;
+    const int64_t b = idx / per;
+    int64_t r = idx - b * per;
+    const int w = (int)(r & 1);
+    r >>= 1;
+    const int64_t ii = r / n2h, kk = r - ii * n2h;
+    int64_t x, y;
+    if (ii > 0) {
+        const int64_t i = ii, j = slices - i;
+        if (kk == 0) {
+            x = i * ss + (w ? n2h * rs : 0);
+            y = j * ss + (w ? n2h * rs : 0);
+        } else {
+            const int64_t k = kk, l = rows - k;
+            x = (w ? j : i) * ss + k * rs;
+            y = (w ? i : j) * ss + l * rs;
+        }
+    } else {
+        if (kk == 0) return;
+        const int64_t k = kk, l = rows - k, base = w ? n1h * ss : 0;
+        x = base + k * rs;
+        y = base + l * rs;
+    }
+    T *p = a + b * dist;
+    if (isgn < 0) {
+        T t = p[x] - p[y];
+        p[x] += p[y];
+        p[y] = t;
+        t = p[y + 1] - p[x + 1];
+        p[x + 1] += p[y + 1];
+        p[y + 1] = t;
+    } else {
+        const T y0 = (T)0.5 * (p[x] - p[y]);
+        p[y] = y0;
+        p[x] -= y0;
+        const T y1 = (T)0.5 * (p[x + 1] + p[y + 1]);
+        p[y + 1] = y1;
+        p[x + 1] -= y1;
+    }
+}
+
 // DHT yTransform, 2D (dht/DoubleDHT_2D.java:1288-1310): each thread owns one
 // (r, c) quadruple with r <= rows/2, c <= cols/2.  Quadruples that alias
 // (r or c on a symmetry line) are processed by one thread in the reference's

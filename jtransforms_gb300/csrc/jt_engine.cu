@@ -105,8 +105,10 @@ template <typename T> static BOp elem_op(int kind, int sign, int64_t total) {
 
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// (a step with no batch-recordable form refuses to be recorded)
 #define LAUNCH1D(ctx, total, kernel, ...)                                              \
     do {                                                                               \
+        if ((ctx).rec) return JT_EINVAL;                                               \
         if (!(ctx).dry && (total) > 0) {                                               \
             int64_t g_ = cdiv((total), 256);                                           \
             auto kfn_ = kernel;                                                        \
@@ -126,6 +128,7 @@ static std::atomic<int> g_opt_tma{1};
 static std::atomic<int> g_opt_colpass{0};
 static std::atomic<int> g_opt_direct_max_f32{8192};
 static std::atomic<int> g_opt_direct_max_f64{8192};
+static std::atomic<int> g_opt_chunk_mb{48};
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
 
@@ -546,7 +549,8 @@ template <typename T> struct Fft1 {
                 return exec_direct(ctx, in, out, batch, li, lo, sign, scale);
             }
             case ALG_TWOPASS: {
-                int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)(48ll << 20) / (n * (int64_t)sizeof(C2))));
+                const int64_t chunk_bytes = (int64_t)g_opt_chunk_mb.load() << 20;
+                int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, chunk_bytes / (n * (int64_t)sizeof(C2))));
                 C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * chunk * n, ctx.dry);
                 for (int64_t b = 0; b < batch; b += chunk) {
                     int64_t cb = std::min(chunk, batch - b);
@@ -956,6 +960,11 @@ template <typename T> struct PlanImpl {
                 JT_TRY(get_real(dims[1], &r));
                 return get_fft(dims[0], &f);
             }
+            if (nd == 3 && (op == JT_REAL_FORWARD || op == JT_REAL_INVERSE)) {
+                JT_TRY(get_real(dims[2], &r));
+                JT_TRY(get_fft(dims[1], &f));
+                return get_fft(dims[0], &f);
+            }
             for (int a = 0; a < nd; a++) JT_TRY(get_fft(dims[a], &f));
             return JT_OK;
         }
@@ -1069,6 +1078,30 @@ template <typename T> struct PlanImpl {
                 }
                 case JT_REAL_FORWARD:
                 case JT_REAL_INVERSE: {
+                    if (nd == 3) {
+                        // fft/DoubleFFT_3D.java:1339-1356, :1629-1645: rows' real
+                        // FFT, complex passes along rows then slices on the
+                        // packed pairs, rdft3d_sub (inverse: the reverse order)
+                        const int64_t S = dims[0], R = dims[1], Cc = dims[2], H = Cc / 2;
+                        Real1<T> *r = real.at(Cc).get();
+                        Fft1<T> *fr = fft.at(R).get();
+                        Fft1<T> *fs = fft.at(S).get();
+                        Layout lr = {H, R * H, 1, H};
+                        Layout ls = {R * H, S * R * H, 1, R * H};
+                        const int64_t pairs = batch * (S / 2) * (R / 2) * 2;
+                        if (op == JT_REAL_FORWARD) {
+                            JT_TRY(r->fwd_packed(ctx, a, Cc, batch * S * R));
+                            JT_TRY(column_fft(ctx, fr, (C2 *)a, batch * S, R, H, lr, -1, 1.0));
+                            JT_TRY(column_fft(ctx, fs, (C2 *)a, batch, S, R * H, ls, -1, 1.0));
+                            LAUNCH1D(ctx, pairs, rdft3d_kernel<T>, a, dist, S, R, Cc, batch, 1);
+                            return JT_OK;
+                        }
+                        LAUNCH1D(ctx, pairs, rdft3d_kernel<T>, a, dist, S, R, Cc, batch, -1);
+                        JT_TRY(column_fft(ctx, fs, (C2 *)a, batch, S, R * H, ls, 1, scale ? 1.0 / (double)S : 1.0));
+                        JT_TRY(column_fft(ctx, fr, (C2 *)a, batch * S, R, H, lr, 1, scale ? 1.0 / (double)R : 1.0));
+                        double factor = scale ? 1.0 : (double)Cc / 2.0;
+                        return r->inv_packed(ctx, a, Cc, batch * S * R, factor);
+                    }
                     if (nd != 2) return JT_EINVAL;
                     const int64_t rows = dims[0], cols = dims[1];
                     Real1<T> *r = real.at(cols).get();
@@ -1236,7 +1269,6 @@ int check_op(const jt_plan *p, int op) {
     if (p->kind == JT_FFT && p->nd > 1 && (op == JT_REAL_FORWARD || op == JT_REAL_INVERSE)) {
         for (int d = 0; d < p->nd; d++)
             if (!is_pow2(p->dims[d])) return JT_ENOTPOW2;
-        if (p->nd == 3) return JT_EINVAL;  // packed 3D real layout: not built yet
     }
     return JT_OK;
 }
@@ -1455,6 +1487,10 @@ int jt_set_option(int option, int value) {
     if (option == JT_OPT_DIRECT_MAX_F32) return g_opt_direct_max_f32.exchange(value);
     if (option == JT_OPT_COLUMN_KERNEL) return g_opt_colpass.exchange(value ? 1 : 0);
     if (option == JT_OPT_DIRECT_MAX_F64) return g_opt_direct_max_f64.exchange(value);
+    if (option == JT_OPT_TWOPASS_CHUNK_MB) {
+        if (value < 1 || value > 1024) return JT_EINVAL;
+        return g_opt_chunk_mb.exchange(value);
+    }
     return JT_EINVAL;
 }
 

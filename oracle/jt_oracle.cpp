@@ -879,6 +879,68 @@ template <class T> void fft2d_real_inverse(T *a, i64 rows, i64 cols, bool sc) {
     for (i64 r = 0; r < rows; r++) fc.realInverse(a + r * cols, sc);
 }
 
+// rdft3d_sub (fft/DoubleFFT_3D.java:6909-7021): combines the (slice, row)
+// mirror pairs of the packed columns 0 and 1.  Each pair is (x, y): forward
+// (isgn >= 0) y = (x - y)/2, x -= y on the real part and y = (x + y)/2,
+// x -= y on the imaginary part; inverse (isgn < 0) x, y = x + y, x - y and
+// x', y' = x' + y', y' - x'.
+template <class T> void rdft3d_sub(T *a, i64 slices, i64 rows, i64 cols, int isgn) {
+    const i64 n1h = slices >> 1, n2h = rows >> 1, ss = rows * cols, rs = cols;
+    auto pair = [&](i64 x, i64 y) {
+        if (isgn >= 0) {
+            a[y] = (T)0.5f * (a[x] - a[y]);
+            a[x] -= a[y];
+            a[y + 1] = (T)0.5f * (a[x + 1] + a[y + 1]);
+            a[x + 1] -= a[y + 1];
+        } else {
+            T t = a[x] - a[y];
+            a[x] += a[y];
+            a[y] = t;
+            t = a[y + 1] - a[x + 1];
+            a[x + 1] += a[y + 1];
+            a[y + 1] = t;
+        }
+    };
+    for (i64 i = 1; i < n1h; i++) {
+        const i64 j = slices - i;
+        pair(i * ss, j * ss);
+        pair(i * ss + n2h * rs, j * ss + n2h * rs);
+        for (i64 k = 1; k < n2h; k++) {
+            const i64 l = rows - k;
+            pair(i * ss + k * rs, j * ss + l * rs);
+            pair(j * ss + k * rs, i * ss + l * rs);
+        }
+    }
+    for (i64 k = 1; k < n2h; k++) {
+        const i64 l = rows - k;
+        pair(k * rs, l * rs);
+        pair(n1h * ss + k * rs, n1h * ss + l * rs);
+    }
+}
+
+// realForward 3D, power-of-two sizes (fft/DoubleFFT_3D.java:1339-1356):
+// row realForward, complexForward along rows then along slices on the
+// packed pairs (xdft3da_sub1(1, -1), cdft3db_sub(-1)), rdft3d_sub(1).
+template <class T> void fft3d_real_forward(T *a, i64 slices, i64 rows, i64 cols) {
+    FFT1D<T> fc(cols), fr(rows), fs(slices);
+    for (i64 r = 0; r < slices * rows; r++) fc.realForward(a + r * cols);
+    i64 dims[3] = {slices, rows, cols / 2};
+    for_lines<T>(a, 3, dims, 1, 2, [&](T *t) { fr.complexForward(t); });
+    for_lines<T>(a, 3, dims, 0, 2, [&](T *t) { fs.complexForward(t); });
+    rdft3d_sub<T>(a, slices, rows, cols, 1);
+}
+
+// realInverse 3D (fft/DoubleFFT_3D.java:1629-1645): rdft3d_sub(-1),
+// complexInverse along slices then rows, row realInverse.
+template <class T> void fft3d_real_inverse(T *a, i64 slices, i64 rows, i64 cols, bool sc) {
+    FFT1D<T> fc(cols), fr(rows), fs(slices);
+    rdft3d_sub<T>(a, slices, rows, cols, -1);
+    i64 dims[3] = {slices, rows, cols / 2};
+    for_lines<T>(a, 3, dims, 0, 2, [&](T *t) { fs.complexInverse(t, sc); });
+    for_lines<T>(a, 3, dims, 1, 2, [&](T *t) { fr.complexInverse(t, sc); });
+    for (i64 r = 0; r < slices * rows; r++) fc.realInverse(a + r * cols, sc);
+}
+
 // realForwardFull / realInverseFull nD: the full complex transform of the
 // real input stored in the first N slots, result in 2N slots.
 template <class T> void fftnd_real_full(T *a, int nd, const i64 *dims, int isign, bool sc) {
@@ -991,12 +1053,16 @@ template <class T> int run_one(int kind, int op, int nd, const i64 *dims, T *a, 
             case OP_REAL_FORWARD_FULL: fftnd_real_full<T>(a, nd, dims, -1, false); return 0;
             case OP_REAL_INVERSE_FULL: fftnd_real_full<T>(a, nd, dims, +1, s); return 0;
             case OP_REAL_FORWARD:
-                if (nd != 2 || !is_pow2(dims[0]) || !is_pow2(dims[1])) return -3;
-                fft2d_real_forward<T>(a, dims[0], dims[1]);
-                return 0;
             case OP_REAL_INVERSE:
-                if (nd != 2 || !is_pow2(dims[0]) || !is_pow2(dims[1])) return -3;
-                fft2d_real_inverse<T>(a, dims[0], dims[1], s);
+                for (int d = 0; d < nd; d++)
+                    if (!is_pow2(dims[d])) return -3;
+                if (nd == 2) {
+                    if (op == OP_REAL_FORWARD) fft2d_real_forward<T>(a, dims[0], dims[1]);
+                    else fft2d_real_inverse<T>(a, dims[0], dims[1], s);
+                } else {
+                    if (op == OP_REAL_FORWARD) fft3d_real_forward<T>(a, dims[0], dims[1], dims[2]);
+                    else fft3d_real_inverse<T>(a, dims[0], dims[1], dims[2], s);
+                }
                 return 0;
             default: return -1;
         }

@@ -78,6 +78,37 @@ def test_fft_2d_real_packed(oracle, prec, shape):
         assert rel_l2(c, d) <= tol(N, dt)
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("shape", [(2, 2, 2), (2, 4, 8), (4, 8, 16), (8, 4, 2), (16, 16, 16), (32, 64, 16),
+                                   (128, 128, 128)])
+def test_fft_3d_real_packed(oracle, prec, shape):
+    """fft/DoubleFFT_3D.java realForward / realInverse packed layout
+    (fft/DoubleFFT_3DTest.java:565-592, :868-895)."""
+    dt = np.float64 if prec == "f64" else np.float32
+    N = int(np.prod(shape))
+    f = _fft_cls(3, prec)(*shape)
+    x = _x(N).astype(dt)
+    a, b = x.copy(), x.copy()
+    f.realForward(a)
+    oracle.run(oracle.FFT, oracle.REAL_FORWARD, list(shape), b)
+    assert rel_l2(a, b) <= tol(N, dt)
+    for s in (True, False):
+        c, d = a.copy(), b.copy()
+        f.realInverse(c, s)
+        oracle.run(oracle.FFT, oracle.REAL_INVERSE, list(shape), d, s)
+        assert rel_l2(c, d) <= tol(N, dt)
+    c = a.copy()
+    f.realInverse(c, True)
+    assert rel_l2(c, x) <= 2 * tol(N, dt)
+
+
+def test_fft_3d_real_requires_pow2():
+    import jtransforms_gb300 as J
+    f = J.DoubleFFT_3D(4, 6, 8)
+    with pytest.raises(J.IllegalArgumentException):
+        f.realForward(np.zeros(192))
+
+
 def test_fft_2d_real_requires_pow2():
     import jtransforms_gb300 as J
     f = J.DoubleFFT_2D(6, 8)

@@ -145,6 +145,99 @@ def test_oracle_2d_real_packed(oracle, shape):
     assert rel_l2(a, x.ravel()) < 1e-14
 
 
+def fill_symmetric_3d(a, slices, rows, cols):
+    """Expands the packed 3D realForward result (first slices*rows*cols
+    values of `a`, length 2*slices*rows*cols) into the full interleaved
+    spectrum, as the reference test does (fft/DoubleFFT_3DTest.java:431-558)."""
+    twon3, n2d2, n1d2 = 2 * cols, rows // 2, slices // 2
+    ss, rs = rows * cols, cols
+    tss, trs = rows * twon3, twon3
+    for s in range(slices - 1, 0, -1):
+        for r in range(rows):
+            for c in range(0, cols, 2):
+                i1, i2 = s * ss + r * rs + c, 2 * s * ss + 2 * r * rs + c
+                a[i2], a[i1] = a[i1], 0
+                a[i2 + 1], a[i1 + 1] = a[i1 + 1], 0
+    for r in range(1, rows):
+        for c in range(0, cols, 2):
+            i1, i2 = (rows - r) * rs + c, (rows - r) * trs + c
+            a[i2], a[i1] = a[i1], 0
+            a[i2 + 1], a[i1 + 1] = a[i1 + 1], 0
+    for s in range(slices):
+        i3, i5 = ((slices - s) % slices) * tss, s * tss
+        for r in range(rows):
+            i4, i6 = ((rows - r) % rows) * trs, r * trs
+            for c in range(1, cols, 2):
+                i1, i2 = i3 + i4 + twon3 - c, i5 + i6 + c
+                a[i1] = -a[i2 + 2]
+                a[i1 - 1] = a[i2 + 1]
+    for s in range(slices):
+        i5, i6 = ((slices - s) % slices) * tss, s * tss
+        for r in range(1, n2d2):
+            i4 = i6 + (rows - r) * trs
+            i1, i2, i3 = i5 + r * trs + cols, i4 + cols, i4 + 1
+            a[i1] = a[i3]
+            a[i2] = a[i3]
+            a[i1 + 1] = -a[i4]
+            a[i2 + 1] = a[i4]
+    for s in range(slices):
+        i3, i4 = ((slices - s) % slices) * tss, s * tss
+        for r in range(1, n2d2):
+            i1, i2 = i3 + (rows - r) * trs, i4 + r * trs
+            a[i1] = a[i2]
+            a[i1 + 1] = -a[i2 + 1]
+    for s in range(1, n1d2):
+        i1, i2, i3 = s * tss, (slices - s) * tss, n2d2 * trs
+        i4, i5 = i1 + i3, i2 + i3
+        a[i1 + cols] = a[i2 + 1]
+        a[i2 + cols] = a[i2 + 1]
+        a[i1 + cols + 1] = -a[i2]
+        a[i2 + cols + 1] = a[i2]
+        a[i4 + cols] = a[i5 + 1]
+        a[i5 + cols] = a[i5 + 1]
+        a[i4 + cols + 1] = -a[i5]
+        a[i5 + cols + 1] = a[i5]
+        a[i2] = a[i1]
+        a[i2 + 1] = -a[i1 + 1]
+        a[i5] = a[i4]
+        a[i5 + 1] = -a[i4 + 1]
+    a[cols] = a[1]
+    a[1] = 0
+    i1, i2 = n2d2 * trs, n1d2 * tss
+    i3 = i1 + i2
+    a[i1 + cols] = a[i1 + 1]
+    a[i1 + 1] = 0
+    a[i2 + cols] = a[i2 + 1]
+    a[i2 + 1] = 0
+    a[i3 + cols] = a[i3 + 1]
+    a[i3 + 1] = 0
+    a[i2 + cols + 1] = 0
+    a[i3 + cols + 1] = 0
+    return a
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (4, 8, 16), (8, 4, 2), (16, 16, 16), (4, 32, 8)])
+def test_oracle_3d_real_packed(oracle, shape):
+    """Pinned like the reference test (fft/DoubleFFT_3DTest.java:565-592):
+    the packed result, expanded by fillSymmetric, equals the full complex
+    forward transform; realInverse(scale) restores the input."""
+    s_, r_, c_ = shape
+    N = s_ * r_ * c_
+    x = np.random.default_rng(3).uniform(0, 1, shape)
+    a = np.zeros(2 * N)
+    a[:N] = x.ravel()
+    oracle.run(oracle.FFT, oracle.REAL_FORWARD, list(shape), a[:N])
+    packed = a[:N].copy()
+    full = fill_symmetric_3d(a, s_, r_, c_)
+    F = np.fft.fftn(x)
+    want = np.empty(2 * N)
+    want[0::2] = F.real.ravel()
+    want[1::2] = F.imag.ravel()
+    assert rel_l2(full, want) < 1e-14
+    oracle.run(oracle.FFT, oracle.REAL_INVERSE, list(shape), packed, True)
+    assert rel_l2(packed, x.ravel()) < 1e-14
+
+
 @pytest.mark.parametrize("dims", [(3, 5), (6, 10), (5, 7, 3), (4, 4, 4), (8, 6, 10)])
 def test_oracle_nd(oracle, dims):
     O = oracle
