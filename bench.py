@@ -462,7 +462,7 @@ def run_ours(args, world, rank, local):
     achieved = bytes_step / (sum(per_size_ms) * 1e-3) / 1e9
     per_size = {f"2^{int(math.log2(n))}": {"ms": ms, "GFLOP/s": flops_c2c(n, ELEMS // n) / (ms * 1e-3) / 1e9,
                                            "GB/s": 2 * 8 * ELEMS / (ms * 1e-3) / 1e9,
-                                           "algorithm": ["direct", "two-pass", "bluestein", "trivial"][plans[i].plan.algorithm(0)]}
+                                           "algorithm": ["direct", "two-pass", "bluestein", "trivial", "three-pass"][plans[i].plan.algorithm(0)]}
                 for i, (n, ms) in enumerate(zip(SIZES, per_size_ms))}
 
     # error against FP64 of one transform per size: input set (a) = the timed
@@ -577,7 +577,7 @@ def main():
     ap.add_argument("--no-tma", action="store_true", help="use the plain (non-TMA) power-of-two kernel")
     ap.add_argument("--direct-max", type=int, default=0, help="longest float length done in one pass")
     ap.add_argument("--no-colpass", action="store_true", help="column passes on the tile-pipelined kernel")
-    ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 48)")
+    ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 1024)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
     args = ap.parse_args()
     global ELEMS, SIZES

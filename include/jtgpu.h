@@ -154,8 +154,11 @@ int jt_batch_destroy(jt_batch *batch);
 #define JT_OPT_DIRECT_MAX_F64 2 /* the same for double (default 8192) */
 #define JT_OPT_COLUMN_KERNEL 3  /* 0 (default): column passes use the tile-pipelined kernel; 1: the
                                    line-group kernel with swizzled TMA tensor loads and stores */
-#define JT_OPT_TWOPASS_CHUNK_MB 4 /* MiB of transforms per two-pass chunk (default 48, 1..1024): the
-                                     column pass's output stays in L2 for the row pass */
+#define JT_OPT_TWOPASS_CHUNK_MB 4 /* MiB of transforms per two-pass chunk and launch (default 1024,
+                                     1..16384); the intermediate scratch is one chunk */
+#define JT_OPT_THREEPASS_MIN_LOG2 5 /* float powers of two from 2^value (up to 2^30) use three
+                                       passes of near-equal lengths (default 21; 0: never).  Read
+                                       when a plan is created. */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 
@@ -165,7 +168,7 @@ int jt_last_cuda_error(void);
 /* Number of kernel launches this thread issued since the last reset. */
 int64_t jt_launch_count(int reset);
 /* Algorithm the plan uses along axis `axis` for length-n complex work:
- * 0 direct in-CTA, 1 two-pass, 2 Bluestein, 3 trivial. */
+ * 0 direct in-CTA, 1 two-pass, 2 Bluestein, 3 trivial, 4 three-pass. */
 int jt_plan_algorithm(const jt_plan *plan, int axis);
 
 #ifdef __cplusplus

@@ -8,7 +8,8 @@
 //   TWOPASS   n = n1 * n2 with both DIRECT: column pass with the four-step
 //             twiddle fused into its store, then a row pass that writes the
 //             transposed (natural-order) result.  The batch is processed in
-//             chunks whose intermediate stays in L2.
+//             chunks of up to 1 GiB: one launch per pass and chunk (long
+//             launches measured faster than L2-sized chunks).
 //   BLUESTEIN everything else: chirp-z with a power-of-two convolution of
 //             nextPow2(2n-1) points (fft/DoubleFFT_1D.java:1864-2107), chirp
 //             tables generated in FP64 on the device.
@@ -128,7 +129,8 @@ static std::atomic<int> g_opt_tma{1};
 static std::atomic<int> g_opt_colpass{0};
 static std::atomic<int> g_opt_direct_max_f32{8192};
 static std::atomic<int> g_opt_direct_max_f64{8192};
-static std::atomic<int> g_opt_chunk_mb{48};
+static std::atomic<int> g_opt_chunk_mb{1024};
+static std::atomic<int64_t> g_opt_threepass_min{(int64_t)1 << 21};
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
 
@@ -204,7 +206,7 @@ static bool make_col_tmap(CUtensorMap *m, const void *base, int esz, int64_t inn
 // ---------------------------------------------------------------------------
 // Complex FFT of one length
 // ---------------------------------------------------------------------------
-enum { ALG_DIRECT = 0, ALG_TWOPASS = 1, ALG_BLUESTEIN = 2, ALG_TRIVIAL = 3 };
+enum { ALG_DIRECT = 0, ALG_TWOPASS = 1, ALG_BLUESTEIN = 2, ALG_TRIVIAL = 3, ALG_THREEPASS = 4 };
 
 static const int kMaxThreads = 512;
 
@@ -242,12 +244,26 @@ template <typename T> struct Fft1 {
     std::unique_ptr<Fft1> pa, pb, pbl;
     C2 *Whi = nullptr, *Wlo = nullptr;
     int lo_bits = 0;
+    // three passes: n = n1 * n2 * n3, the row length m = n2 * n3 split again
+    int64_t n3 = 0;
+    std::unique_ptr<Fft1> pc;
+    C2 *Whi2 = nullptr, *Wlo2 = nullptr;  // four-step twiddle of length m
+    int lo_bits2 = 0;
     int64_t nB = 0;
     C2 *bk1 = nullptr, *bk2 = nullptr;
 
     ~Fft1() {
-        for (void *p : {(void *)W, (void *)Wp, (void *)Whi, (void *)Wlo, (void *)bk1, (void *)bk2})
+        for (void *p : {(void *)W, (void *)Wp, (void *)Whi, (void *)Wlo, (void *)Whi2, (void *)Wlo2, (void *)bk1, (void *)bk2})
             if (p) cudaFree(p);
+    }
+
+    // two-level table of w_len^e, e < len: Whi[e >> bits] * Wlo[e & (2^bits - 1)]
+    static int make_twiddle_pair(int64_t len, C2 **hi, C2 **lo, int *bits) {
+        *bits = 0;
+        while (((int64_t)1 << (2 * *bits)) < len) (*bits)++;
+        const int64_t nlo = (int64_t)1 << *bits;
+        JT_TRY(make_roots(lo, nlo, 1, len));
+        return make_roots(hi, cdiv(len, nlo), nlo, len);
     }
 
     static bool generic_ok(int64_t n) { return n >= 2 && n <= Lim<T>::lmax() && !direct_radices(n).empty(); }
@@ -300,6 +316,23 @@ template <typename T> struct Fft1 {
             JT_TRY(f->set_reg(reg_ok(n)));
             if (!f->reg) f->radix = direct_radices(n);
             JT_TRY(make_roots(&f->W, n, 1, n));
+        } else if (sizeof(T) == 4 && is_pow2(n) && g_opt_threepass_min.load() > 0 && n >= g_opt_threepass_min.load() &&
+                   n <= ((int64_t)1 << 30)) {  // twiddle exponents stay below 2^31
+            // three register-kernel passes of lengths as equal as possible
+            // (2^24 = 256^3): every pass runs 128-byte-wide column tiles,
+            // where a 4096 x 4096 split would run 16-byte ones
+            int lg = 0;
+            while (((int64_t)1 << lg) < n) lg++;
+            const int a = lg / 3, b = (lg - a) / 2, c = lg - a - b;
+            f->algo = ALG_THREEPASS;
+            f->n1 = (int64_t)1 << a;
+            f->n2 = (int64_t)1 << b;
+            f->n3 = (int64_t)1 << c;
+            JT_TRY(create(f->n1, f->pa));
+            JT_TRY(create(f->n2, f->pb));
+            JT_TRY(create(f->n3, f->pc));
+            JT_TRY(make_twiddle_pair(n, &f->Whi, &f->Wlo, &f->lo_bits));
+            JT_TRY(make_twiddle_pair(f->n2 * f->n3, &f->Whi2, &f->Wlo2, &f->lo_bits2));
         } else {
             // two DIRECT lengths, n = n1 (column pass) * n2 (row pass): as
             // balanced as possible, preferring lengths both passes run on
@@ -558,6 +591,31 @@ template <typename T> struct Fft1 {
                     JT_TRY(pa->exec_direct(ctx, in + b * din, tmp, cb * n2, lai, lao, sign, 1.0, n, n2, Whi, Wlo, lo_bits, 0, 0));
                     Layout lbi = {n1, n, n2, 1}, lbo = {n1, dout, 1, n1};
                     JT_TRY(pb->exec_direct(ctx, tmp, out + b * dout, cb * n1, lbi, lbo, sign, scale, 0, 1, nullptr, nullptr, 0, 1, 1));
+                }
+                return JT_OK;
+            }
+            case ALG_THREEPASS: {
+                if (ctx.rec) return JT_EINVAL;  // batches record lengths up to the tile kernel's
+                const int64_t m = n2 * n3;
+                const int64_t chunk_bytes = (int64_t)g_opt_chunk_mb.load() << 20;
+                int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, chunk_bytes / (n * (int64_t)sizeof(C2))));
+                C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * chunk * n, ctx.dry);
+                for (int64_t b = 0; b < batch; b += chunk) {
+                    int64_t cb = std::min(chunk, batch - b);
+                    // A: n1-point columns of the n1 x m view, twiddle w_n^{k1 c}
+                    Layout lai = {m, din, 1, m}, lao = {m, n, 1, m};
+                    JT_TRY(pa->exec_direct(ctx, in + b * din, tmp, cb * m, lai, lao, sign, 1.0, n, m, Whi, Wlo, lo_bits, 0, 0));
+                    // B1: n2-point columns of each row's n2 x n3 view, twiddle
+                    // w_m^{t u}, in place (a tile is in shared memory before
+                    // any of its columns is written)
+                    Layout lb = {n3, m, 1, n3};
+                    JT_TRY(pb->exec_direct(ctx, tmp, tmp, cb * n1 * n3, lb, lb, sign, 1.0, m, n3, Whi2, Wlo2, lo_bits2, 0, 0));
+                    // B2: n3-point rows, written to X[k1 + n1 (t + n2 v)];
+                    // line k1 + n1 t of one transform per launch
+                    Layout lci = {n1, n3, m, 1}, lco = {n1, n1, 1, n1 * n2};
+                    for (int64_t t = 0; t < cb; t++)
+                        JT_TRY(pc->exec_direct(ctx, tmp + t * n, out + (b + t) * dout, n1 * n2, lci, lco, sign, scale, 0, 1,
+                                               nullptr, nullptr, 0, 1, 1));
                 }
                 return JT_OK;
             }
@@ -1487,8 +1545,15 @@ int jt_set_option(int option, int value) {
     if (option == JT_OPT_DIRECT_MAX_F32) return g_opt_direct_max_f32.exchange(value);
     if (option == JT_OPT_COLUMN_KERNEL) return g_opt_colpass.exchange(value ? 1 : 0);
     if (option == JT_OPT_DIRECT_MAX_F64) return g_opt_direct_max_f64.exchange(value);
+    if (option == JT_OPT_THREEPASS_MIN_LOG2) {
+        if (value < 0 || value > 30) return JT_EINVAL;
+        const int64_t prev = g_opt_threepass_min.exchange(value ? (int64_t)1 << value : 0);
+        int lg = 0;
+        while (prev && ((int64_t)1 << lg) < prev) lg++;
+        return prev ? lg : 0;
+    }
     if (option == JT_OPT_TWOPASS_CHUNK_MB) {
-        if (value < 1 || value > 1024) return JT_EINVAL;
+        if (value < 1 || value > 16384) return JT_EINVAL;
         return g_opt_chunk_mb.exchange(value);
     }
     return JT_EINVAL;
@@ -1767,7 +1832,7 @@ static int noalloc_run(jt_plan *p, int op, const void *in, void *out, int64_t ba
     if (it == im->fft.end()) return JT_EINVAL;  // tables are built by jt_plan_create
     Fft1<T> *f = it->second.get();
     if (f->algo == ALG_BLUESTEIN) return JT_ESCRATCH;
-    const int64_t per = f->algo == ALG_TWOPASS ? n * (int64_t)sizeof(C2) : 0;
+    const int64_t per = (f->algo == ALG_TWOPASS || f->algo == ALG_THREEPASS) ? n * (int64_t)sizeof(C2) : 0;
     if (per > (int64_t)JT_NOALLOC_SCRATCH_BYTES) return JT_ESCRATCH;
     void *scratch = nullptr;
     JT_TRY(noalloc_scratch(&scratch));
