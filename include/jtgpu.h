@@ -162,6 +162,13 @@ int jt_batch_destroy(jt_batch *batch);
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 
+/* Pass split of power-of-two length 2^log2n in `prec` for plans created from
+ * now on, overriding the compiled plan table (the autotuner's probe):
+ * (0,0,0) one pass; (a,b,0) two passes 2^a x 2^b, a + b = log2n, each <= 12;
+ * (a,b,c) three passes (Float32 only), a + b + c = log2n; a < 0 clears the
+ * override.  No counterpart in the reference. */
+int jt_set_split(int prec, int log2n, int a, int b, int c);
+
 /* Diagnostics ------------------------------------------------------------ */
 const char *jt_strerror(int status);
 int jt_last_cuda_error(void);

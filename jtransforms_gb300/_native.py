@@ -33,6 +33,7 @@ SIGNATURES = {
     "jt_plan_destroy": (_I, [_P]),
     "jt_plan_extent": (_I, [_P, _I, ctypes.POINTER(_L)]),
     "jt_plan_set_mode": (_I, [_P, _I]),
+    "jt_set_split": (_I, [_I, _I, _I, _I, _I]),
     "jt_execute": (_I, [_P, _I, _P, _L, _L, _I]),
     "jt_execute_batch": (_I, [_P, _I, _P, _L, _L, _L, _L, _I]),
     "jt_execute_device": (_I, [_P, _I, _P, _L, _L, _I, _P]),

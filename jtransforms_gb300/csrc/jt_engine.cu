@@ -16,6 +16,7 @@
 #include "jt_device.cuh"
 #include "jt_stockham.cuh"
 #include "jt_batch.cuh"
+#include "jt_plan_table.h"
 #include "../../include/jtgpu.h"
 
 #include <cuda.h>
@@ -131,6 +132,14 @@ static std::atomic<int> g_opt_direct_max_f32{8192};
 static std::atomic<int> g_opt_direct_max_f64{8192};
 static std::atomic<int> g_opt_chunk_mb{1024};
 static std::atomic<int64_t> g_opt_threepass_min{(int64_t)1 << 21};
+// pass-split overrides (jt_set_split), [precision][log2 n]; a < 0: none
+#define JT_SPLIT_MAX_LOG2 30
+static signed char g_split_override[2][JT_SPLIT_MAX_LOG2 + 1][3];
+static bool g_split_override_init = [] {
+    for (auto &p : g_split_override)
+        for (auto &e : p) e[0] = e[1] = e[2] = -1;
+    return true;
+}();
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
 
@@ -305,34 +314,85 @@ template <typename T> struct Fft1 {
         return JT_OK;
     }
 
-    static int create(int64_t n, std::unique_ptr<Fft1> &out) {
+    // Pass split of a power-of-two length from jt_set_split's override or
+    // the measured plan table (jt_plan_table.h): {0,0,0} one pass, {a,b,0}
+    // two passes 2^a x 2^b, {a,b,c} three passes; nullptr: the rules below.
+    static const signed char *table_split(int64_t n) {
+        int lg = 0;
+        while (((int64_t)1 << lg) < n) lg++;
+        if (lg > JT_SPLIT_MAX_LOG2) return nullptr;
+        const int pi = sizeof(T) == 4 ? 0 : 1;
+        const signed char *o = g_split_override[pi][lg];
+        if (o[0] >= 0) return o;
+        const signed char *t = sizeof(T) == 4 ? kSplitF32[lg] : kSplitF64[lg];
+        return t[0] >= 0 ? t : nullptr;
+    }
+
+    int init_direct() {
+        algo = ALG_DIRECT;
+        JT_TRY(set_reg(reg_ok(n)));
+        if (!reg) radix = direct_radices(n);
+        return make_roots(&W, n, 1, n);
+    }
+
+    // n = n1 (column pass, four-step twiddle fused) x n2 (transposing row pass)
+    int init_twopass(int64_t d) {
+        algo = ALG_TWOPASS;
+        n1 = d;
+        n2 = n / d;
+        JT_TRY(create(n1, pa, false));
+        JT_TRY(create(n2, pb, false));
+        // pass A reads and writes columns, pass B writes columns: the
+        // register kernel does that up to 4096, the generic one always
+        for (Fft1 *sub : {pa.get(), pb.get()})
+            if (sub->reg && sub->n > 4096) {
+                sub->reg = false;
+                sub->radix = direct_radices(sub->n);
+            }
+        return make_twiddle_pair(n, &Whi, &Wlo, &lo_bits);
+    }
+
+    // n = n1 x (n2 x n3): column pass A, column pass B1 of each row's
+    // n2 x n3 view, transposing row pass B2 (register kernel, <= 4096 each)
+    int init_threepass(int64_t a, int64_t b, int64_t c) {
+        algo = ALG_THREEPASS;
+        n1 = a;
+        n2 = b;
+        n3 = c;
+        JT_TRY(create(n1, pa, false));
+        JT_TRY(create(n2, pb, false));
+        JT_TRY(create(n3, pc, false));
+        JT_TRY(make_twiddle_pair(n, &Whi, &Wlo, &lo_bits));
+        return make_twiddle_pair(n2 * n3, &Whi2, &Wlo2, &lo_bits2);
+    }
+
+    // top: a transform of its own (its pass split may come from the plan
+    // table); sub-plans are the line passes of a two- or three-pass plan
+    static int create(int64_t n, std::unique_ptr<Fft1> &out, bool top = true) {
         std::unique_ptr<Fft1> f(new (std::nothrow) Fft1());
         if (!f) return JT_ENOMEM;
         f->n = n;
+        const signed char *sp = (top && n > 16 && is_pow2(n)) ? table_split(n) : nullptr;
         if (n == 1) {
             f->algo = ALG_TRIVIAL;
+        } else if (sp && sp[0] == 0 && reg_ok(n)) {
+            JT_TRY(f->init_direct());
+        } else if (sp && sp[0] > 0 && sp[2] == 0 && sp[0] <= 12 && sp[1] <= 12) {
+            JT_TRY(f->init_twopass((int64_t)1 << sp[0]));
+        } else if (sp && sp[2] > 0 && sizeof(T) == 4 && n <= ((int64_t)1 << 30) && sp[0] <= 12 && sp[1] <= 12 &&
+                   sp[2] <= 12) {  // twiddle exponents stay below 2^31
+            JT_TRY(f->init_threepass((int64_t)1 << sp[0], (int64_t)1 << sp[1], (int64_t)1 << sp[2]));
         } else if (direct_ok(n) && (!is_pow2(n) || n <= one_pass_max())) {
-            f->algo = ALG_DIRECT;
-            JT_TRY(f->set_reg(reg_ok(n)));
-            if (!f->reg) f->radix = direct_radices(n);
-            JT_TRY(make_roots(&f->W, n, 1, n));
+            JT_TRY(f->init_direct());
         } else if (sizeof(T) == 4 && is_pow2(n) && g_opt_threepass_min.load() > 0 && n >= g_opt_threepass_min.load() &&
-                   n <= ((int64_t)1 << 30)) {  // twiddle exponents stay below 2^31
+                   n <= ((int64_t)1 << 30)) {
             // three register-kernel passes of lengths as equal as possible
             // (2^24 = 256^3): every pass runs 128-byte-wide column tiles,
             // where a 4096 x 4096 split would run 16-byte ones
             int lg = 0;
             while (((int64_t)1 << lg) < n) lg++;
             const int a = lg / 3, b = (lg - a) / 2, c = lg - a - b;
-            f->algo = ALG_THREEPASS;
-            f->n1 = (int64_t)1 << a;
-            f->n2 = (int64_t)1 << b;
-            f->n3 = (int64_t)1 << c;
-            JT_TRY(create(f->n1, f->pa));
-            JT_TRY(create(f->n2, f->pb));
-            JT_TRY(create(f->n3, f->pc));
-            JT_TRY(make_twiddle_pair(n, &f->Whi, &f->Wlo, &f->lo_bits));
-            JT_TRY(make_twiddle_pair(f->n2 * f->n3, &f->Whi2, &f->Wlo2, &f->lo_bits2));
+            JT_TRY(f->init_threepass((int64_t)1 << a, (int64_t)1 << b, (int64_t)1 << c));
         } else {
             // two DIRECT lengths, n = n1 (column pass) * n2 (row pass): as
             // balanced as possible, preferring lengths both passes run on
@@ -349,23 +409,7 @@ template <typename T> struct Fft1 {
                 if (dd < bestd) { bestd = dd; best = d; }
             }
             if (best) {
-                f->algo = ALG_TWOPASS;
-                f->n1 = best;
-                f->n2 = n / best;
-                JT_TRY(create(f->n1, f->pa));
-                JT_TRY(create(f->n2, f->pb));
-                // pass A reads and writes columns, pass B writes columns: the
-                // register kernel does that up to 4096, the generic one always
-                for (Fft1 *sub : {f->pa.get(), f->pb.get()})
-                    if (sub->reg && sub->n > 4096) {
-                        sub->reg = false;
-                        sub->radix = direct_radices(sub->n);
-                    }
-                f->lo_bits = 0;
-                while (((int64_t)1 << (2 * f->lo_bits)) < n) f->lo_bits++;
-                int64_t nlo = (int64_t)1 << f->lo_bits;
-                JT_TRY(make_roots(&f->Wlo, nlo, 1, n));
-                JT_TRY(make_roots(&f->Whi, cdiv(n, nlo), nlo, n));
+                JT_TRY(f->init_twopass(best));
             } else {
                 f->algo = ALG_BLUESTEIN;
                 f->nB = next_pow2(2 * n - 1);
@@ -1239,8 +1283,15 @@ struct jt_plan {
 
 namespace {
 
+// host-array calls move pieces of the batch through a ring of device
+// buffers: copy in (stream h2d), transform (stream), copy out (stream d2h)
+#define JT_HOST_RING 3
+#define JT_HOST_PIECE_BYTES (128ll << 20)
+
 struct ThreadState {
     cudaStream_t stream = nullptr;
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaEvent_t in_done[JT_HOST_RING] = {}, run_done[JT_HOST_RING] = {}, out_done[JT_HOST_RING] = {};
     Arena arena;
     cudaEvent_t done = nullptr;
     cudaStream_t last = nullptr;
@@ -1254,6 +1305,19 @@ int ensure_stream() {
     if (!t_state.stream) {
         JT_CU(cudaStreamCreateWithFlags(&t_state.stream, cudaStreamNonBlocking));
         JT_CU(cudaEventCreateWithFlags(&t_state.done, cudaEventDisableTiming));
+    }
+    return JT_OK;
+}
+
+int ensure_copy_streams() {
+    if (!t_state.h2d) {
+        JT_CU(cudaStreamCreateWithFlags(&t_state.h2d, cudaStreamNonBlocking));
+        JT_CU(cudaStreamCreateWithFlags(&t_state.d2h, cudaStreamNonBlocking));
+        for (int r = 0; r < JT_HOST_RING; r++) {
+            JT_CU(cudaEventCreateWithFlags(&t_state.in_done[r], cudaEventDisableTiming));
+            JT_CU(cudaEventCreateWithFlags(&t_state.run_done[r], cudaEventDisableTiming));
+            JT_CU(cudaEventCreateWithFlags(&t_state.out_done[r], cudaEventDisableTiming));
+        }
     }
     return JT_OK;
 }
@@ -1341,13 +1405,20 @@ int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t 
     if (off + (batch - 1) * dist + ext > len) return JT_ESHORTBUF;
     JT_TRY(device_init());
     JT_TRY(ensure_stream());
+    JT_TRY(ensure_copy_streams());
     cudaStream_t s = t_state.stream;
     // device copy laid out densely at distance ext (even, for complex views)
     int64_t dd = (ext + 1) & ~(int64_t)1;
     if (p->nd > 1) dd = ext;
     PlanImpl<T> *im = impl_of<T>(p);
     JT_TRY(im->prepare(op));
-    // size: array + scratch (dry run)
+    // pieces of about 128 MiB, up to JT_HOST_RING of them in flight: the copy
+    // in of piece i+1 and the copy out of piece i-1 overlap the transform of i
+    const int64_t per = (int64_t)sizeof(T) * dd;
+    const int64_t piece = std::max<int64_t>(1, std::min<int64_t>(batch, JT_HOST_PIECE_BYTES / per));
+    const int64_t npieces = (batch + piece - 1) / piece;
+    const int ring = (int)std::min<int64_t>(JT_HOST_RING, npieces);
+    // size: ring buffers + one piece's scratch (dry run)
     Ctx c;
     c.s = s;
     c.tc = p->mode == JT_MODE_TC_SPLIT;
@@ -1355,32 +1426,54 @@ int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t 
     c.dry = true;
     t_state.arena.used = 0;
     t_state.arena.peak = 0;
-    T *dev = (T *)t_state.arena.get(sizeof(T) * dd * batch, true);
+    for (int r = 0; r < ring; r++) t_state.arena.get(per * piece, true);
     std::lock_guard<std::mutex> g(im->mu);
-    JT_TRY(im->run(c, op, dev, batch, dd, scale != 0));
+    JT_TRY(im->run(c, op, (T *)nullptr, piece, dd, scale != 0));
     JT_TRY(ensure_arena(t_state.arena.peak));
     if (t_state.last && t_state.last != s) {
         JT_CU(cudaEventRecord(t_state.done, t_state.last));
         JT_CU(cudaStreamWaitEvent(s, t_state.done, 0));
     }
+    // the copy streams start after earlier work on this thread's arena
+    JT_CU(cudaEventRecord(t_state.done, s));
+    JT_CU(cudaStreamWaitEvent(t_state.h2d, t_state.done, 0));
+    JT_CU(cudaStreamWaitEvent(t_state.d2h, t_state.done, 0));
     t_state.arena.used = 0;
     c.dry = false;
-    dev = (T *)t_state.arena.get(sizeof(T) * dd * batch, false);
+    T *buf[JT_HOST_RING];
+    for (int r = 0; r < ring; r++) buf[r] = (T *)t_state.arena.get(per * piece, false);
+    const size_t mark = t_state.arena.used;
     T *h = (T *)host + off;
-    // extent for input: ops whose input is n reals in a 2n output region still
-    // copy the whole extent (the reference reads only the first n).
-    if (dist == dd || batch == 1) {
-        JT_CU(cudaMemcpyAsync(dev, h, sizeof(T) * ((batch - 1) * dd + ext), cudaMemcpyHostToDevice, s));
-    } else {
-        JT_CU(cudaMemcpy2DAsync(dev, sizeof(T) * dd, h, sizeof(T) * dist, sizeof(T) * ext, batch, cudaMemcpyHostToDevice, s));
+    auto copy = [&](T *dst, const T *src, int64_t nb, cudaMemcpyKind kind, cudaStream_t st) -> int {
+        const bool to_dev = kind == cudaMemcpyHostToDevice;
+        if (dist == dd || nb == 1) {
+            JT_CU(cudaMemcpyAsync(dst, src, sizeof(T) * ((nb - 1) * dd + ext), kind, st));
+        } else {
+            JT_CU(cudaMemcpy2DAsync(dst, sizeof(T) * (to_dev ? dd : dist), src, sizeof(T) * (to_dev ? dist : dd),
+                                    sizeof(T) * ext, nb, kind, st));
+        }
+        return JT_OK;
+    };
+    for (int64_t i = 0; i < npieces; i++) {
+        const int r = (int)(i % ring);
+        const int64_t b0 = i * piece, nb = std::min(piece, batch - b0);
+        // buffer r is free once the copy out of piece i - ring finished
+        if (i >= ring) JT_CU(cudaStreamWaitEvent(t_state.h2d, t_state.out_done[r], 0));
+        JT_TRY(copy(buf[r], h + b0 * dist, nb, cudaMemcpyHostToDevice, t_state.h2d));
+        JT_CU(cudaEventRecord(t_state.in_done[r], t_state.h2d));
+        JT_CU(cudaStreamWaitEvent(s, t_state.in_done[r], 0));
+        t_state.arena.used = mark;  // the pieces run in order on one stream: one scratch region
+        JT_TRY(im->run(c, op, buf[r], nb, dd, scale != 0));
+        JT_CU(cudaEventRecord(t_state.run_done[r], s));
+        JT_CU(cudaStreamWaitEvent(t_state.d2h, t_state.run_done[r], 0));
+        JT_TRY(copy(h + b0 * dist, buf[r], nb, cudaMemcpyDeviceToHost, t_state.d2h));
+        JT_CU(cudaEventRecord(t_state.out_done[r], t_state.d2h));
     }
-    JT_TRY(im->run(c, op, dev, batch, dd, scale != 0));
-    if (dist == dd || batch == 1) {
-        JT_CU(cudaMemcpyAsync(h, dev, sizeof(T) * ((batch - 1) * dd + ext), cudaMemcpyDeviceToHost, s));
-    } else {
-        JT_CU(cudaMemcpy2DAsync(h, sizeof(T) * dist, dev, sizeof(T) * dd, sizeof(T) * ext, batch, cudaMemcpyDeviceToHost, s));
-    }
+    // later work on this thread's arena (on any stream) follows the copies out
+    JT_CU(cudaEventRecord(t_state.done, t_state.d2h));
+    JT_CU(cudaStreamWaitEvent(s, t_state.done, 0));
     t_state.last = s;
+    JT_CU(cudaStreamSynchronize(t_state.d2h));
     JT_CU(cudaStreamSynchronize(s));
     JT_CU(cudaGetLastError());
     return check_err_flag();
@@ -1539,6 +1632,23 @@ const char *jt_strerror(int s) {
 }
 
 int jt_last_cuda_error(void) { return g_last_cuda; }
+
+int jt_set_split(int prec, int log2n, int a, int b, int c) {
+    if ((prec != JT_FLOAT32 && prec != JT_FLOAT64) || log2n < 4 || log2n > JT_SPLIT_MAX_LOG2) return JT_EINVAL;
+    signed char *e = g_split_override[prec == JT_FLOAT32 ? 0 : 1][log2n];
+    if (a < 0) {
+        e[0] = e[1] = e[2] = -1;
+        return JT_OK;
+    }
+    const bool one = a == 0 && b == 0 && c == 0;
+    const bool two = a >= 1 && b >= 1 && c == 0 && a <= 12 && b <= 12 && a + b == log2n;
+    const bool three = prec == JT_FLOAT32 && a >= 1 && b >= 1 && c >= 1 && a <= 12 && b <= 12 && c <= 12 && a + b + c == log2n;
+    if (!one && !two && !three) return JT_EINVAL;
+    e[0] = (signed char)a;
+    e[1] = (signed char)b;
+    e[2] = (signed char)c;
+    return JT_OK;
+}
 
 int jt_set_option(int option, int value) {
     if (option == JT_OPT_TMA_PIPELINE) return g_opt_tma.exchange(value ? 1 : 0);

@@ -120,6 +120,38 @@ def test_offsets_and_bounds(oracle, prec, n):
         f.complexForward(np.zeros(2 * n, np.float32 if dt == np.float64 else np.float64))
 
 
+@pytest.mark.parametrize("prec,n,batch,gap,op", [("f32", 1024, 50000, 0, "cf"), ("f32", 1024, 20001, 6, "cf"),
+                                                ("f64", 4096, 5000, 2, "ci"), ("f32", 1 << 20, 40, 0, "rf"),
+                                                ("f64", 1000, 3, 4, "cf")])
+def test_host_batch_pieces(prec, n, batch, gap, op):
+    """jt_execute_batch on a host array of many pieces (copy in, transform and
+    copy out overlapped through a ring of device buffers), with and without a
+    gap between arrays and an offset: identical to the device-array path."""
+    import torch
+    from jtransforms_gb300 import _native as N
+    dt = np.float64 if prec == "f64" else np.float32
+    cls = _classes()[prec][1]
+    f = cls(n)
+    ext = n if op == "rf" else 2 * n
+    dist = ext + gap
+    off = 3
+    code = {"cf": N.COMPLEX_FORWARD, "ci": N.COMPLEX_INVERSE, "rf": N.REAL_FORWARD}[op]
+    rng = np.random.default_rng(n + batch)
+    host = rng.uniform(-1, 1, off + dist * batch).astype(dt)
+    keep = host.copy()
+    f.plan.execute(code, host, off, op == "ci", batch=batch, dist=dist)
+    dense = np.stack([keep[off + b * dist: off + b * dist + ext] for b in range(batch)])
+    dev = torch.from_numpy(dense.ravel().copy()).cuda()
+    f.plan.execute(code, dev, 0, op == "ci", batch=batch, dist=ext)
+    got = np.stack([host[off + b * dist: off + b * dist + ext] for b in range(batch)])
+    assert np.array_equal(got, dev.cpu().numpy().reshape(batch, ext))
+    # the gaps and the prefix are untouched
+    assert np.array_equal(host[:off], keep[:off])
+    for b in range(min(batch, 50)):
+        s = off + b * dist + ext
+        assert np.array_equal(host[s:s + gap], keep[s:s + gap])
+
+
 @pytest.mark.parametrize("n", [4096, 1000, 4099])
 def test_round_trips(n):
     """complexForward then complexInverse(scale) and realForward then

@@ -1,8 +1,8 @@
-"""GPU parity of the large Float lengths (three passes from 2^21 up, two
-passes below): complexForward / complexInverse against an FP64 FFT of the
-same input and against the two-pass plan, and realForward of a length whose
-half-length complex FFT takes three passes.  Tolerance: relative L2 <=
-4 * eps_float * log2(n) (the benchmark spec bound, against FP64)."""
+"""GPU parity of the pass splits of large Float lengths: the compiled plan
+table's choice (two or three passes) and every split kind forced through
+jt_set_split, against an FP64 FFT of the same input; realForward of a length
+whose half-length FFT runs three passes.  Tolerance: relative L2 <=
+4 * eps_float * log2(n) against FP64 (the benchmark spec bound)."""
 import numpy as np
 import pytest
 
@@ -21,14 +21,9 @@ def _fp64_fft(x, n, inverse=False, scale=False):
     return out
 
 
-@pytest.mark.parametrize("lg,batch", [(21, 2), (22, 1), (23, 1), (24, 1)])
-def test_three_pass_complex(lg, batch):
-    import jtransforms_gb300 as J
+def _check(f, n, batch, seed):
     from jtransforms_gb300 import _native as N
-    n = 1 << lg
-    f = J.FloatFFT_1D(n)
-    assert f.plan.algorithm(0) == 4  # three passes
-    x = np.random.default_rng(lg).standard_normal(2 * n * batch).astype(np.float32)
+    x = np.random.default_rng(seed).standard_normal(2 * n * batch).astype(np.float32)
     a = x.copy()
     f.plan.execute(N.COMPLEX_FORWARD, a, 0, False, batch=batch, dist=2 * n)
     assert rel_l2(a, _fp64_fft(x, n)) <= tol(n, np.float32)
@@ -38,22 +33,41 @@ def test_three_pass_complex(lg, batch):
         assert rel_l2(c, _fp64_fft(x, n, inverse=True, scale=s)) <= tol(n, np.float32)
 
 
-def test_three_pass_matches_two_pass():
+@pytest.mark.parametrize("lg,batch", [(21, 2), (22, 1), (23, 1), (24, 1)])
+def test_table_split_large(lg, batch):
+    import jtransforms_gb300 as J
+    f = J.FloatFFT_1D(1 << lg)
+    assert f.plan.algorithm(0) in (1, 4)  # two or three passes
+    _check(f, 1 << lg, batch, lg)
+
+
+# one entry per split kind: one pass, two passes either way round, three
+# passes with short and long first passes, lengths up to 4096 per pass
+FORCED = [(14, (0, 0, 0), 0), (14, (4, 10, 0), 1), (16, (12, 4, 0), 1), (18, (9, 9, 0), 1), (18, (6, 6, 6), 4),
+          (20, (4, 6, 10), 4), (21, (7, 7, 7), 4), (22, (11, 11, 0), 1), (22, (10, 6, 6), 4), (24, (12, 12, 0), 1)]
+
+
+@pytest.mark.parametrize("lg,split,algo", FORCED)
+def test_forced_split(lg, split, algo):
     import jtransforms_gb300 as J
     from jtransforms_gb300 import _native as N
-    n = 1 << 22
-    x = np.random.default_rng(5).standard_normal(2 * n).astype(np.float32)
-    a = x.copy()
-    J.FloatFFT_1D(n).complexForward(a)
-    prev = N.set_option(N.OPT_THREEPASS_MIN_LOG2, 0)
+    lib = N.load()
+    assert lib.jt_set_split(N.FLOAT32, lg, *split) == N.OK
     try:
-        g = J.FloatFFT_1D(n)
-        assert g.plan.algorithm(0) == 1  # two passes
-        b = x.copy()
-        g.complexForward(b)
+        f = J.FloatFFT_1D(1 << lg)
     finally:
-        N.set_option(N.OPT_THREEPASS_MIN_LOG2, prev)
-    assert rel_l2(a, b) <= tol(n, np.float32)
+        lib.jt_set_split(N.FLOAT32, lg, -1, 0, 0)
+    assert f.plan.algorithm(0) == algo
+    _check(f, 1 << lg, 2 if lg <= 20 else 1, 100 + lg)
+
+
+def test_set_split_rules():
+    from jtransforms_gb300 import _native as N
+    lib = N.load()
+    assert lib.jt_set_split(N.FLOAT32, 20, 10, 9, 0) == N.EINVAL      # sums to 19
+    assert lib.jt_set_split(N.FLOAT32, 26, 13, 13, 0) == N.EINVAL     # a pass above 4096
+    assert lib.jt_set_split(N.FLOAT64, 24, 8, 8, 8) == N.EINVAL       # three passes: Float32 only
+    assert lib.jt_set_split(N.FLOAT32, 31, 0, 0, 0) == N.EINVAL
 
 
 def test_three_pass_real_forward():
