@@ -38,8 +38,9 @@ HEADLINE_SIZES = list(SIZES)
 # DRAM bytes (read + write) of one headline step, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, L2 kept between launches) of
 # the 256 MiB-per-size case, scaled by 4 (traffic grows with the transforms
-# processed): 2142 + 2205 + 2178 + 2250 + 3065 MB for 2^10 .. 2^24
-TRAFFIC_PER_STEP = 11.84e9
+# processed): 2142 + 4012 + 3882 + 3924 + 6120 MB for 2^10 .. 2^24 (one pass,
+# two passes, two, two, three: each pass reads and writes the array)
+TRAFFIC_PER_STEP = 20.08e9
 ELEMS = 2 ** 27          # complex elements per size per rank (1 GiB complex64)
 SEED = 20110602
 METRIC = "GFLOP/s (5N log2N) & % HBM roofline; TC-split vs plain FP32 at same error"
@@ -215,6 +216,35 @@ def timed_calls(fn_list, restore, flush, steps, warmup, stream):
                 times[i].append((e0, e1))
     torch.cuda.synchronize()
     return [[a.elapsed_time(b) for a, b in t] for t in times]
+
+
+def link_bandwidth(host_np, dev):
+    """Host<->device copy bandwidth of a 1 GiB pinned array (GB/s): one
+    direction at a time, and both at once on two streams (the bound of the
+    end-to-end leg, whose copies in and out overlap)."""
+    import torch
+    h = torch.from_numpy(host_np)
+    d = torch.empty_like(dev)
+    d2 = torch.empty_like(dev)
+    h2 = torch.empty(h.numel(), dtype=h.dtype, pin_memory=True)
+    nbytes = h.numel() * h.element_size()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    out = {}
+    for name in ("h2d", "d2h", "bidirectional"):
+        best = 1e9
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if name in ("h2d", "bidirectional"):
+                with torch.cuda.stream(s1):
+                    d.copy_(h, non_blocking=True)
+            if name in ("d2h", "bidirectional"):
+                with torch.cuda.stream(s2):
+                    h2.copy_(d2, non_blocking=True)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        out[name] = (2 if name == "bidirectional" else 1) * nbytes / best / 1e9
+    return out
 
 
 def sixty_db(n, gen):
@@ -411,6 +441,8 @@ def run_ours(args, world, rank, local):
         N.set_option(N.OPT_COLUMN_KERNEL, 0)
     if args.chunk_mb:
         N.set_option(N.OPT_TWOPASS_CHUNK_MB, args.chunk_mb)
+    if args.host_piece_mb:
+        N.set_option(N.OPT_HOST_PIECE_MB, args.host_piece_mb)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -499,10 +531,10 @@ def run_ours(args, world, rank, local):
     del set_b
 
     # end to end through the C ABI with pinned host buffers
-    e2e_val = None
+    e2e_val, link = None, None
     del work
     if not args.no_e2e:
-        e2e_steps = max(1, min(args.steps, 3))
+        e2e_steps = max(1, min(args.steps, 5))
         host = []
         for i, n in enumerate(SIZES):
             h = torch.empty(2 * ELEMS, dtype=torch.float32, pin_memory=True)
@@ -517,6 +549,7 @@ def run_ours(args, world, rank, local):
                 plans[i].plan.execute(N.COMPLEX_FORWARD, host[i], 0, False, batch=ELEMS // n, dist=2 * n)
         e2e_s = (time.perf_counter() - t0) / e2e_steps
         e2e_val = flops_step / e2e_s / 1e9
+        link = link_bandwidth(host[0], pristine[0])
         del host
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -540,7 +573,10 @@ def run_ours(args, world, rank, local):
                          "applies_to": "row passes of length 16..2048 (direct sizes); longer lengths run plain passes"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * ELEMS * len(SIZES),
                     "d2h_bytes_per_step": 8 * ELEMS * len(SIZES),
-                    "path": "FloatFFT_1D plan -> jt_execute_batch on pinned host arrays"},
+                    "path": "FloatFFT_1D plan -> jt_execute_batch on pinned host arrays",
+                    "link_GBps": link,
+                    "link_bound_GFLOP/s": (flops_step / (8 * ELEMS * len(SIZES) / (link["bidirectional"] / 2 * 1e9)) / 1e9
+                                           if link else None)},
             "gpu_launches": launches,
             "timed_wall_s": wall}
     clocks = clk.summary(t_wall0, t_wall1)
@@ -578,6 +614,7 @@ def main():
     ap.add_argument("--direct-max", type=int, default=0, help="longest float length done in one pass")
     ap.add_argument("--no-colpass", action="store_true", help="column passes on the tile-pipelined kernel")
     ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 1024)")
+    ap.add_argument("--host-piece-mb", type=int, default=0, help="MiB per piece of the end-to-end host batch (library default 64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
     args = ap.parse_args()
     global ELEMS, SIZES

@@ -156,6 +156,8 @@ int jt_batch_destroy(jt_batch *batch);
                                    line-group kernel with swizzled TMA tensor loads and stores */
 #define JT_OPT_TWOPASS_CHUNK_MB 4 /* MiB of transforms per two-pass chunk and launch (default 1024,
                                      1..16384); the intermediate scratch is one chunk */
+#define JT_OPT_HOST_PIECE_MB 6   /* MiB per piece of a host-array batch (default 64, 1..16384):
+                                    pieces are copied in, transformed and copied out overlapped */
 #define JT_OPT_THREEPASS_MIN_LOG2 5 /* float powers of two from 2^value (up to 2^30) use three
                                        passes of near-equal lengths (default 21; 0: never).  Read
                                        when a plan is created. */

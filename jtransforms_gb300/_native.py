@@ -51,7 +51,7 @@ SIGNATURES = {
     "jt_execute_device_noalloc": (_I, [_P, _I, _P, _P, _L, _I, _P]),
 }
 OPT_TMA_PIPELINE, OPT_DIRECT_MAX_F32, OPT_DIRECT_MAX_F64, OPT_COLUMN_KERNEL, OPT_TWOPASS_CHUNK_MB = 0, 1, 2, 3, 4
-OPT_THREEPASS_MIN_LOG2 = 5
+OPT_THREEPASS_MIN_LOG2, OPT_HOST_PIECE_MB = 5, 6
 
 _lib = None
 _lock = threading.Lock()

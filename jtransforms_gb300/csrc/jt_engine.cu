@@ -131,6 +131,7 @@ static std::atomic<int> g_opt_colpass{0};
 static std::atomic<int> g_opt_direct_max_f32{8192};
 static std::atomic<int> g_opt_direct_max_f64{8192};
 static std::atomic<int> g_opt_chunk_mb{1024};
+static std::atomic<int> g_opt_host_piece_mb{64};
 static std::atomic<int64_t> g_opt_threepass_min{(int64_t)1 << 21};
 // pass-split overrides (jt_set_split), [precision][log2 n]; a < 0: none
 #define JT_SPLIT_MAX_LOG2 30
@@ -496,7 +497,7 @@ template <typename T> struct Fft1 {
             if (lin.estride == 1 && lout.estride == 1) mode = 0;
             else if (lin.estride != 1 && lout.estride != 1 && n <= 4096) mode = 1;
             else if (lin.estride == 1 && lout.estride != 1 && n <= 4096) mode = 2;
-            if (mode < 0 || (mode == 0 && tw_n != 0)) return JT_EINVAL;  // the four-step twiddle rides on column passes
+            if (mode < 0 || (mode != 1 && tw_n != 0)) return JT_EINVAL;  // the four-step twiddle rides on column passes
             StockParams sp;
             memset(&sp, 0, sizeof(sp));
             sp.nlines = nlines;
@@ -1286,7 +1287,6 @@ namespace {
 // host-array calls move pieces of the batch through a ring of device
 // buffers: copy in (stream h2d), transform (stream), copy out (stream d2h)
 #define JT_HOST_RING 3
-#define JT_HOST_PIECE_BYTES (128ll << 20)
 
 struct ThreadState {
     cudaStream_t stream = nullptr;
@@ -1412,10 +1412,12 @@ int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t 
     if (p->nd > 1) dd = ext;
     PlanImpl<T> *im = impl_of<T>(p);
     JT_TRY(im->prepare(op));
-    // pieces of about 128 MiB, up to JT_HOST_RING of them in flight: the copy
-    // in of piece i+1 and the copy out of piece i-1 overlap the transform of i
+    // pieces of about JT_OPT_HOST_PIECE_MB, up to JT_HOST_RING of them in
+    // flight: the copy in of piece i+1 and the copy out of piece i-1 overlap
+    // the transform of piece i
     const int64_t per = (int64_t)sizeof(T) * dd;
-    const int64_t piece = std::max<int64_t>(1, std::min<int64_t>(batch, JT_HOST_PIECE_BYTES / per));
+    const int64_t piece_bytes = (int64_t)g_opt_host_piece_mb.load() << 20;
+    const int64_t piece = std::max<int64_t>(1, std::min<int64_t>(batch, piece_bytes / per));
     const int64_t npieces = (batch + piece - 1) / piece;
     const int ring = (int)std::min<int64_t>(JT_HOST_RING, npieces);
     // size: ring buffers + one piece's scratch (dry run)
@@ -1661,6 +1663,10 @@ int jt_set_option(int option, int value) {
         int lg = 0;
         while (prev && ((int64_t)1 << lg) < prev) lg++;
         return prev ? lg : 0;
+    }
+    if (option == JT_OPT_HOST_PIECE_MB) {
+        if (value < 1 || value > 16384) return JT_EINVAL;
+        return g_opt_host_piece_mb.exchange(value);
     }
     if (option == JT_OPT_TWOPASS_CHUNK_MB) {
         if (value < 1 || value > 16384) return JT_EINVAL;

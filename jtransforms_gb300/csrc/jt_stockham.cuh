@@ -9,7 +9,8 @@
 //   MODE 1  columns in, columns out  (C adjacent columns per tile), optional
 //           four-step twiddle fused into the store
 //   MODE 2  rows in, columns out     (the transposing row pass of the
-//           four-step scheme; the store is staged through shared memory)
+//           four-step scheme; lines are spread across a warp, so one store
+//           instruction writes C adjacent columns)
 //
 // stockham_pipe_kernel is the main kernel: persistent CTAs walk their tiles
 // and the next tile is already in flight while the current one is computed.
@@ -18,7 +19,7 @@
 // C columns x up to 256 rows (MODE 1), completing on an mbarrier.  Every
 // mbarrier wait is bounded; on timeout the kernel raises the error flag,
 // drains its copies (bounded) and returns.  The passes exchange through the
-// stage buffer itself with an XOR swizzle.
+// stage buffer itself, in padded rows (one spare slot per 16 elements).
 // stockham_kernel is the plain (non-TMA) variant for arrays whose addresses
 // or strides do not meet TMA's 16-byte rules.
 #pragma once
@@ -142,7 +143,11 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     // pipelined kernel: two stages of C padded lines (TMA fills the first
     // C*L elements densely; the exchange uses the padded layout) and two
     // mbarriers
-    static constexpr int STAGE = ((C * LP + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
+    // MODE 2 copies each input line to its own row of even stride (16-byte
+    // aligned for the bulk copy); the exchange then runs inside that row
+    static constexpr int LPS = LP + (LP & 1);
+    static constexpr int ROW = MODE == 2 ? LPS : LP;
+    static constexpr int STAGE = ((C * ROW + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
     static constexpr size_t PIPE_SMEM = 2 * (size_t)STAGE * sizeof(C2) + 16;
     static constexpr bool PIPE_OK = PIPE_SMEM <= 227 * 1024;
     // blocks per SM the register budget is sized for (about 24 warps)
@@ -357,9 +362,10 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
     C2 *stage1 = stage0 + S::STAGE;
     uint64_t *bar = reinterpret_cast<uint64_t *>(stage1 + S::STAGE);
     const int tid = threadIdx.x;
-    // MODE 1 walks across columns (c fastest); MODE 0/2 walk along rows
+    // the column modes walk across lines (c fastest: a warp's stores of one
+    // output position cover C adjacent columns); MODE 0 walks along rows
     int c, t;
-    if (MODE == 1) {
+    if (MODE != 0) {
         c = tid % S::C;
         t = tid / S::C;
     } else {
@@ -386,6 +392,12 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             mbar_arrive_expect_tx(mb, (uint32_t)(S::C * L * ESZ));
 #pragma unroll 1
             for (int r = 0; r < L; r += BR) tensor3d_g2s_hint(st + r * S::C, &tmap, col0 * XM, r, (int)ob, mb, pol);
+        } else if (MODE == 2) {
+            // one row of stride ROW per line
+            mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
+#pragma unroll 1
+            for (int cc = 0; cc < lines; cc++)
+                bulk_g2s_hint(st + cc * S::ROW, in + line_off(p.lin, b0 + cc), (uint32_t)(L * ESZ), mb, pol);
         } else if (p.lin.inner == 1 && p.lin.outer == L) {
             // C consecutive contiguous rows: one copy
             mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
@@ -410,7 +422,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
 
     // the four-step twiddle belongs to the column pass (the launcher never
     // asks the row mode for one)
-    const bool tw = MODE != 0 && p.tw_n != 0;
+    const bool tw = MODE == 1 && p.tw_n != 0;
     const int lo_mask = (1 << p.tw_lo_bits) - 1;
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
@@ -446,28 +458,11 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             for (int m = 0; m < S::E; m++) v[m] = st[(t + m * S::TL) * S::C + c];
         } else {
 #pragma unroll
-            for (int m = 0; m < S::E; m++) v[m] = st[c * L + t + m * S::TL];
+            for (int m = 0; m < S::E; m++) v[m] = st[c * (MODE == 2 ? S::ROW : L) + t + m * S::TL];
         }
         __syncthreads();  // every pass-0 read is done before the exchange writes
-        PadIdx xi{c * S::LP};
-        if (MODE == 2) {
-            // last pass to shared memory, then a column-coalesced store: the
-            // thread's column cc is fixed, positions advance by NT / C
-            auto store_s = [&](int pos, C2 val, int) { st[xi(pos)] = val; };
-            S::run_all(v, t, st, xi, W, store_s);
-            __syncthreads();
-            const int cc = tid % S::C;
-            if (b0 + cc < p.nlines) {
-                C2 *o = out + line_off(p.lout, b0 + cc);
-                const C2 *srow = st + cc * S::LP;
-#pragma unroll 4
-                for (int pos = tid / S::C; pos < L; pos += S::NT / S::C) {
-                    C2 val = srow[pad(pos)];
-                    if (do_scale) val = cscale<T>(val, sc);
-                    st_hint(&o[(int64_t)pos * oes32], val, spol);
-                }
-            }
-        } else {
+        PadIdx xi{c * S::ROW};
+        {
             C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
             const int j2 = tw ? (int)(b % p.tw_inner) : 0;
             // Four-step twiddle w^{pos*j2}: the last pass writes pos = t + TL*m,
