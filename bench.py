@@ -132,6 +132,36 @@ def dist_setup(args):
     return world, rank, local
 
 
+# Replicas: every rank transforms its own batch (weak scaling); the only
+# cross-rank traffic is the start barrier and the max of the step times.
+def dist_init(world: int, backend: str = "nccl"):
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend)
+
+
+def dist_barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_finish(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 # ----------------------------------------------------------------------------
 # reference arm: the oracle (CPU restatement of JTransforms) on host cores
 # ----------------------------------------------------------------------------
@@ -443,9 +473,7 @@ def run_ours(args, world, rank, local):
         N.set_option(N.OPT_TWOPASS_CHUNK_MB, args.chunk_mb)
     if args.host_piece_mb:
         N.set_option(N.OPT_HOST_PIECE_MB, args.host_piece_mb)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist_init(world, "nccl")
     peak, peak_src = measured_peaks()
     stream = torch.cuda.current_stream()
     flushbuf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -468,9 +496,7 @@ def run_ours(args, world, rank, local):
     clk = ClockSampler(local).__enter__()  # running before the warm-up: samples cover the timed region
     # warm-up (tables, scratch, clocks)
     timed_calls(fns, lambda i: work[i].copy_(pristine[i]), flush, 0, args.warmup, stream)
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    dist_barrier(world)
     torch.cuda.synchronize()
     J.launch_count(reset=True)
     t_wall0 = time.perf_counter()
@@ -483,11 +509,7 @@ def run_ours(args, world, rank, local):
     clk.__exit__(None, None, None)
     per_size_ms = [sum(t) / len(t) for t in times]
     step_ms = sum(per_size_ms)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        step_ms = float(tt.item())
+    step_ms = max_over_ranks(step_ms, world, "cuda")
     flops_step = sum(flops_c2c(n, ELEMS // n) for n in SIZES) * world
     value = flops_step / (step_ms * 1e-3) / 1e9
     bytes_step = 2 * 8 * ELEMS * len(SIZES)
@@ -593,9 +615,7 @@ def run_ours(args, world, rank, local):
             line["other_workloads_error"] = repr(e)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    dist_finish(world)
     return 0
 
 

@@ -144,7 +144,10 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     // C*L elements densely; the exchange uses the padded layout) and two
     // mbarriers
     // MODE 2 copies each input line to its own row of even stride (16-byte
-    // aligned for the bulk copy); the exchange then runs inside that row
+    // aligned for the bulk copy); the exchange then runs inside that row.
+    // (A stride chosen to spread the column modes' exchange over all banks
+    // halves their shared-memory wavefronts at L = 1024, 2048 but measured
+    // slower: it costs residency at L = 128 and gained nothing at 1024.)
     static constexpr int LPS = LP + (LP & 1);
     static constexpr int ROW = MODE == 2 ? LPS : LP;
     static constexpr int STAGE = ((C * ROW + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
