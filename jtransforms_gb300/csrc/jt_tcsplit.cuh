@@ -15,14 +15,20 @@
 // 2^-17 residual per operand, too coarse for the 1e-6 bound.)
 //
 // Twiddles, the head/remainder split and the final short radix (L not a
-// power of 16) stay on the CUDA cores in FP32.  Between passes the outputs
-// go through the padded exchange buffer (aliasing the A operands, which are
-// dead once the products completed), as in the register kernel.
+// power of 16) stay on the CUDA cores in FP32.  From the first radix-16 pass
+// to the second each thread twiddles its own 16 outputs (they all feed input
+// k' = 16 t / (L/16) of the next pass, so their factors w_256^{k k'} are one
+// row of the pass table) and writes them straight into the next pass's A
+// rows; before a final short radix the outputs go through the padded
+// exchange buffer (aliasing the A operands, dead once their products
+// completed), as in the register kernel.
 //
-// Operands are K-major without swizzle: core matrices of 8 rows x 16 bytes,
-// element (r, k) of a K = 32 operand at byte
-//     (r / 8) * 1024 + (k / 4) * 128 + (r % 8) * 16 + (k % 4) * 4,
-// i.e. leading-dimension offset 128 (K direction), stride offset 1024.
+// Operands are K-major without swizzle: core matrices of 8 rows x 16 bytes.
+// A: element (r, k) at byte (r / 8) * 1168 + (k / 4) * 144 + (r % 8) * 16 +
+// (k % 4) * 4 (leading offset 144, stride offset 1168): the 16-byte skews
+// put both the own-row writes and the scattered next-pass writes of a warp
+// on every bank slot equally (minimum wavefronts).  B: leading offset 128,
+// stride offset 1024.
 #pragma once
 
 #include "jt_stockham.cuh"
@@ -68,10 +74,13 @@ template <int L> struct TcCfg {
     static constexpr int LOGL = ilog2c(L);
     static constexpr int NTC = LOGL / 4;  // radix-16 passes on the tensor cores
     static constexpr int LP = L + L / 16 + 1;
-    static constexpr int OFF_AHI = 0, OFF_ALO = 16384, OFF_B = 32768;  // B: heads 4 KB, remainders 4 KB
-    static constexpr int OFF_BAR = 40960, OFF_TM = OFF_BAR + 8;
+    static constexpr int A_LBO = 144, A_SBO = 1168, A_BYTES = 16 * A_SBO;
+    static constexpr int OFF_AHI = 0, OFF_ALO = A_BYTES, OFF_B = 2 * A_BYTES;  // B: heads 4 KB, remainders 4 KB
+    static constexpr int OFF_BAR = OFF_B + 8192, OFF_TM = OFF_BAR + 8;
     static constexpr int SMEM = OFF_BAR + 64;
-    static constexpr bool OK = L >= 16 && L <= 2048 && (size_t)C * LP * 8 <= 32768;
+    // byte offset of 16-byte chunk q (K elements 4q..4q+3) of A row r
+    static __device__ __forceinline__ int aoff(int r, int q) { return (r >> 3) * A_SBO + q * A_LBO + (r & 7) * 16; }
+    static constexpr bool OK = L >= 16 && L <= 2048 && (size_t)C * LP * 8 <= 2 * A_BYTES;
 };
 
 template <int L, int SIGN> struct TcPass {
@@ -86,15 +95,8 @@ template <int L, int SIGN> struct TcPass {
                                                uint32_t taddr, uint64_t *bar, uint32_t &phase, const PadIdx &xi,
                                                const float2 *__restrict__ W, Store &store) {
         typedef typename S::template Pass<s> PP;
-        if constexpr (s > 0) {
-            float2 tw[S::template Tw<s>::N];
-            S::template load_tw<s>(t, W, tw);
-#pragma unroll
-            for (int k = 1; k < 16; k++) v[k] = SIGN < 0 ? cmul<float>(v[k], tw[k - 1]) : cmulc<float>(v[k], tw[k - 1]);
-        }
-        __syncthreads();  // the exchange buffer (aliasing A) has been read
-        {
-            const int arow = (tid >> 3) * 1024 + (tid & 7) * 16;
+        if constexpr (s == 0) {
+            __syncthreads();  // the previous tile's exchange (aliasing A) has been read
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 float4 h, l;
@@ -102,25 +104,28 @@ template <int L, int SIGN> struct TcPass {
                 tf32_split(v[2 * q].y, h.y, l.y);
                 tf32_split(v[2 * q + 1].x, h.z, l.z);
                 tf32_split(v[2 * q + 1].y, h.w, l.w);
-                *reinterpret_cast<float4 *>(sm + K::OFF_AHI + arow + q * 128) = h;
-                *reinterpret_cast<float4 *>(sm + K::OFF_ALO + arow + q * 128) = l;
+                *reinterpret_cast<float4 *>(sm + K::OFF_AHI + K::aoff(tid, q)) = h;
+                *reinterpret_cast<float4 *>(sm + K::OFF_ALO + K::aoff(tid, q)) = l;
             }
         }
+        // (pass s > 0: the previous pass wrote this pass's A rows directly)
         fence_proxy_async_smem();
         tc_fence_before();
         __syncthreads();
         if (tid == 0) {
             tc_fence_after();
             constexpr uint32_t IDESC = umma_idesc_tf32(128, 32);
-            // K step ks starts 2 core matrices (256 bytes = 16 units) further
-            const uint64_t ahi = umma_desc(sbase + K::OFF_AHI, 128, 1024), alo = umma_desc(sbase + K::OFF_ALO, 128, 1024);
+            const uint64_t ahi = umma_desc(sbase + K::OFF_AHI, K::A_LBO, K::A_SBO);
+            const uint64_t alo = umma_desc(sbase + K::OFF_ALO, K::A_LBO, K::A_SBO);
             const uint64_t bhi = umma_desc(sbase + K::OFF_B, 128, 1024), blo = umma_desc(sbase + K::OFF_B + 4096, 128, 1024);
 #pragma unroll
             for (int pr = 0; pr < 3; pr++) {
                 const uint64_t a = pr == 1 ? alo : ahi;
                 const uint64_t b = pr == 2 ? blo : bhi;
+                // K step ks starts 2 core matrices further: 2 * LBO bytes (16-byte units)
 #pragma unroll
-                for (int ks = 0; ks < 4; ks++) umma_tf32(tmem, a + ks * 16, b + ks * 16, IDESC, (pr | ks) != 0);
+                for (int ks = 0; ks < 4; ks++)
+                    umma_tf32(tmem, a + ks * (2 * K::A_LBO / 16), b + ks * (2 * 128 / 16), IDESC, (pr | ks) != 0);
             }
             umma_commit(bar);
         }
@@ -140,6 +145,37 @@ template <int L, int SIGN> struct TcPass {
             for (int k = 0; k < 16; k++) store(idxD + k * PP::NS, make_float2(r[2 * k], r[2 * k + 1]), k);
             tc_fence_before();
             return true;
+        } else if constexpr (!LAST_TC) {
+            // first radix-16 pass -> second: output k of butterfly t is input
+            // k' = 16 t / TL of butterfly j' = (16 t + k) mod TL of the next
+            // pass (s = 0: idxD = 16 t), with factor w_256^{(j' mod 16) k'} =
+            // w_256^{k k'}: row k' of the pass-1 table (the table is symmetric)
+            static_assert(s == 0 && PP::NS == 1, "direct writes follow the first pass");
+            const int kp = (16 * t) / K::TL;
+            const int c = tid / K::TL;
+            const float4 *row = reinterpret_cast<const float4 *>(W + S::template twoff<1>() + kp * 16);
+            float2 tw[16];
+#pragma unroll
+            for (int k2 = 0; k2 < 8; k2++) {
+                const float4 x = __ldg(row + k2);
+                tw[2 * k2] = make_float2(x.x, x.y);
+                tw[2 * k2 + 1] = make_float2(x.z, x.w);
+            }
+            const int colb = K::aoff(0, kp >> 1) + (kp & 1) * 8;  // chunk of column pair k', row 0
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                float2 u = make_float2(r[2 * k], r[2 * k + 1]);
+                if (k > 0) u = SIGN < 0 ? cmul<float>(u, tw[k]) : cmulc<float>(u, tw[k]);
+                const int rp = c * K::TL + ((16 * t + k) & (K::TL - 1));
+                const int off = colb + (rp >> 3) * K::A_SBO + (rp & 7) * 16;
+                float2 h, l;
+                tf32_split(u.x, h.x, l.x);
+                tf32_split(u.y, h.y, l.y);
+                *reinterpret_cast<float2 *>(sm + K::OFF_AHI + off) = h;
+                *reinterpret_cast<float2 *>(sm + K::OFF_ALO + off) = l;
+            }
+            tc_fence_before();
+            return run<s + 1>(v, t, tid, sm, sbase, tmem, taddr, bar, phase, xi, W, store);
         } else {
             float2 *xs = reinterpret_cast<float2 *>(sm + K::OFF_AHI);
             if constexpr (PP::NS % 16 == 0 || PP::NS == 1) {
@@ -161,16 +197,12 @@ template <int L, int SIGN> struct TcPass {
 #pragma unroll
                 for (int m = 0; m < 16; m++) v[m] = xs[xi(t + m * K::TL)];
             }
-            if constexpr (!LAST_TC) {
-                return run<s + 1>(v, t, tid, sm, sbase, tmem, taddr, bar, phase, xi, W, store);
-            } else {
-                // final short radix on the CUDA cores (its pass reads no shared memory)
-                float2 tw[S::template Tw<K::NTC>::N];
-                S::template load_tw<K::NTC>(t, W, tw);
-                auto nosync = [] {};
-                S::template run<K::NTC>(v, tw, t, xs, xi, W, store, nosync);
-                return true;
-            }
+            // final short radix on the CUDA cores (its pass reads no shared memory)
+            float2 tw[S::template Tw<K::NTC>::N];
+            S::template load_tw<K::NTC>(t, W, tw);
+            auto nosync = [] {};
+            S::template run<K::NTC>(v, tw, t, xs, xi, W, store, nosync);
+            return true;
         }
     }
 };
