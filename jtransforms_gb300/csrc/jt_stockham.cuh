@@ -353,7 +353,8 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT)
 // ---------------------------------------------------------------------------
 #define JT_MBAR_POLL_LIMIT (1u << 22)
 
-template <typename T, int L, int MODE, int SIGN>
+// TW: the column pass fuses the four-step output twiddle (MODE 1 only).
+template <typename T, int L, int MODE, int SIGN, bool TW>
 __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L, MODE, SIGN>::MINB)
     stockham_pipe_kernel(const typename V2<T>::t *__restrict__ in, typename V2<T>::t *__restrict__ out, StockParams p,
                          const __grid_constant__ CUtensorMap tmap, const typename V2<T>::t *__restrict__ W,
@@ -423,9 +424,9 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
     int64_t tile = blockIdx.x;
     if (tid == 0 && tile < ntiles) issue(tile, stage0, &bar[0]);
 
-    // the four-step twiddle belongs to the column pass (the launcher never
-    // asks the row mode for one)
-    const bool tw = MODE == 1 && p.tw_n != 0;
+    // the four-step twiddle belongs to the column pass (the launcher picks
+    // the TW variant from tw_n)
+    constexpr bool tw = MODE == 1 && TW;
     const int lo_mask = (1 << p.tw_lo_bits) - 1;
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
@@ -445,7 +446,8 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         }
         const int64_t b0 = tile * S::C;
         const int64_t b = b0 + c;
-        const bool valid = b < p.nlines;
+        // column tiles are whole (the launcher requires nlines % C == 0)
+        const bool valid = MODE == 1 || b < p.nlines;
         if (MODE == 2 && p.discard_in) {
             // the intermediate rows are now in shared memory and dead in L2
             const int lines = (int)min((int64_t)S::C, p.nlines - b0);
@@ -518,39 +520,39 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
 // Host-side launcher for one (T, L).
 template <typename T, int L> struct StockLaunch {
     typedef typename V2<T>::t C2;
+    template <int MODE, int SIGN, bool TW>
+    static void pipe(const C2 *in, C2 *out, const StockParams &p, const CUtensorMap &tmap, const C2 *W, const C2 *Whi,
+                     const C2 *Wlo, int *err, int sms, cudaStream_t s, int64_t ntiles) {
+        typedef Stockham<T, L, MODE, SIGN> S;
+        auto kern = stockham_pipe_kernel<T, L, MODE, SIGN, TW && MODE == 1>;
+        static int per_sm = 0;
+        if (!per_sm) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::PIPE_SMEM);
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::NT, S::PIPE_SMEM);
+            if (per_sm < 1) per_sm = 1;
+            // shared memory for exactly the resident blocks; the rest of
+            // the SM's 256 KB stays L1, which holds the twiddle tables
+            const int need = per_sm * ((int)S::PIPE_SMEM + 1024);
+            const int pct = (need * 100 + 228 * 1024 - 1) / (228 * 1024);
+            if (pct < 100) {
+                cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+                int again = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&again, kern, S::NT, S::PIPE_SMEM);
+                if (again < per_sm) cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            }
+        }
+        const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * per_sm);
+        kern<<<(unsigned)grid, S::NT, S::PIPE_SMEM, s>>>(in, out, p, tmap, W, Whi, Wlo, err);
+    }
     template <int MODE, int SIGN> static void one(const C2 *in, C2 *out, const StockParams &p, const CUtensorMap *tmap,
                                                   const C2 *W, const C2 *Whi, const C2 *Wlo, int *err, int sms,
                                                   cudaStream_t s) {
         typedef Stockham<T, L, MODE, SIGN> S;
         int64_t ntiles = (p.nlines + S::C - 1) / S::C;
         if constexpr (S::PIPE_OK) if (tmap) {
-            static int per_sm = 0;
-            if (!per_sm) {
-                cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)S::PIPE_SMEM);
-                cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     100);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stockham_pipe_kernel<T, L, MODE, SIGN>, S::NT,
-                                                              S::PIPE_SMEM);
-                if (per_sm < 1) per_sm = 1;
-                // shared memory for exactly the resident blocks; the rest of
-                // the SM's 256 KB stays L1, which holds the twiddle tables
-                const int need = per_sm * ((int)S::PIPE_SMEM + 1024);
-                const int pct = (need * 100 + 228 * 1024 - 1) / (228 * 1024);
-                if (pct < 100) {
-                    cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                         pct);
-                    int again = 0;
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&again, stockham_pipe_kernel<T, L, MODE, SIGN>, S::NT,
-                                                                  S::PIPE_SMEM);
-                    if (again < per_sm)
-                        cudaFuncSetAttribute(stockham_pipe_kernel<T, L, MODE, SIGN>,
-                                             cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-                }
-            }
-            int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * per_sm);
-            stockham_pipe_kernel<T, L, MODE, SIGN>
-                <<<(unsigned)grid, S::NT, S::PIPE_SMEM, s>>>(in, out, p, *tmap, W, Whi, Wlo, err);
+            if (MODE == 1 && p.tw_n != 0) pipe<MODE, SIGN, true>(in, out, p, *tmap, W, Whi, Wlo, err, sms, s, ntiles);
+            else pipe<MODE, SIGN, false>(in, out, p, *tmap, W, Whi, Wlo, err, sms, s, ntiles);
             return;
         }
         static bool attr = false;

@@ -19,6 +19,7 @@ fft/FloatFFT_3D.java (src/main/java/org/jtransforms/).
 """
 from __future__ import annotations
 
+from . import _arrays
 from . import _native as N
 from ._native import IllegalArgumentException
 
@@ -38,8 +39,7 @@ class _FFTBase:
         self._plan = N.Plan(N.FFT, self._prec, dims)
 
     def _run(self, op, a, offa=0, scale=False):
-        return self._plan.execute(op, a.reshape(-1) if hasattr(a, "reshape") and getattr(a, "ndim", 1) > 1 else a,
-                                  offa, scale)
+        return _arrays.run(self._plan, op, a, offa, scale)
 
     # Java methods -----------------------------------------------------
     def complexForward(self, a, offa: int = 0):

@@ -16,6 +16,7 @@ dht/DoubleDHT_3D.java and the Float* twins.
 """
 from __future__ import annotations
 
+from . import _arrays
 from . import _native as N
 from ._native import IllegalArgumentException
 
@@ -44,9 +45,7 @@ class _R2RBase:
         self._plan = N.Plan(self._kind, self._prec, dims)
 
     def _run(self, op, a, offa, scale):
-        if getattr(a, "ndim", 1) > 1:
-            a = a.reshape(-1)
-        return self._plan.execute(op, a, offa, scale)
+        return _arrays.run(self._plan, op, a, offa, scale)
 
     @property
     def plan(self) -> N.Plan:

@@ -102,6 +102,56 @@ def test_fft_3d_real_packed(oracle, prec, shape):
     assert rel_l2(c, x) <= 2 * tol(N, dt)
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_jagged_rows(prec):
+    """double[][] / double[][][] overloads (fft/DoubleFFT_2D.java:345,
+    fft/DoubleFFT_3D.java:542, dct/DoubleDCT_2D.java:104): lists of row
+    arrays give the flat array's results, realForwardFull reads the first
+    half of each 2*columns row (fft/DoubleFFT_2D.java:1010-1021)."""
+    import jtransforms_gb300 as J
+    dt = np.float64 if prec == "f64" else np.float32
+    rows, cols = 8, 16
+    f = _fft_cls(2, prec)(rows, cols)
+    x = _x(2 * rows * cols).astype(dt)
+    flat = x.copy()
+    f.complexForward(flat)
+    jag = [x[r * 2 * cols:(r + 1) * 2 * cols].copy() for r in range(rows)]
+    f.complexForward(jag)
+    assert np.array_equal(np.concatenate(jag), flat)
+    # packed real, rows of `cols`
+    xr = x[: rows * cols].copy()
+    flat = xr.copy()
+    f.realForward(flat)
+    jag = [xr[r * cols:(r + 1) * cols].copy() for r in range(rows)]
+    f.realForward(jag)
+    assert np.array_equal(np.concatenate(jag), flat)
+    # full real: input in the first half of each 2*cols row
+    flat = np.zeros(2 * rows * cols, dt)
+    flat[: rows * cols] = xr
+    f.realForwardFull(flat)
+    jag = [np.concatenate([xr[r * cols:(r + 1) * cols], np.zeros(cols, dt)]) for r in range(rows)]
+    f.realForwardFull(jag)
+    assert np.array_equal(np.concatenate(jag), flat)
+    # 3D nested lists and a 2D DCT of rows
+    g = _fft_cls(3, prec)(4, 2, 8)
+    y = _x(2 * 64).astype(dt)
+    flat = y.copy()
+    g.complexForward(flat)
+    nest = [[y[(s * 2 + r) * 16:(s * 2 + r + 1) * 16].copy() for r in range(2)] for s in range(4)]
+    g.complexForward(nest)
+    assert np.array_equal(np.concatenate([row for sl in nest for row in sl]), flat)
+    d = getattr(J, ("Double" if prec == "f64" else "Float") + "DCT_2D")(rows, cols)
+    flat = xr.copy()
+    d.forward(flat, True)
+    jag = [xr[r * cols:(r + 1) * cols].copy() for r in range(rows)]
+    d.forward(jag, True)
+    assert np.array_equal(np.concatenate(jag), flat)
+    with pytest.raises(TypeError):
+        f.complexForward([np.zeros(2 * cols, np.float32 if dt == np.float64 else np.float64)] * rows)
+    with pytest.raises(J.IllegalArgumentException):
+        f.complexForward(jag, 2)
+
+
 def test_fft_3d_real_requires_pow2():
     import jtransforms_gb300 as J
     f = J.DoubleFFT_3D(4, 6, 8)
