@@ -143,14 +143,28 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     // pipelined kernel: two stages of C padded lines (TMA fills the first
     // C*L elements densely; the exchange uses the padded layout) and two
     // mbarriers
-    // MODE 2 copies each input line to its own row of even stride (16-byte
-    // aligned for the bulk copy); the exchange then runs inside that row.
-    // (A stride chosen to spread the column modes' exchange over all banks
-    // halves their shared-memory wavefronts at L = 1024, 2048 but measured
-    // slower: it costs residency at L = 128 and gained nothing at 1024.)
+    // Exchange stride of the column modes.  A 64-bit shared access is served
+    // per half-warp, whose 16 threads are 16/C positions t x C lines c
+    // (c fastest); they hit 16 distinct 8-byte bank slots when
+    // gcd(stride, 16) = 16 / C, so every exchange access takes the minimum
+    // two wavefronts.  MODE 0 keeps LP (a warp stays inside one line).
+    static constexpr int col_x() {
+        int r = L + L / 16;
+        while (true) {
+            int g = 16, a = r;
+            while (a % 2 == 0 && g > 1) { a /= 2; g /= 2; }  // g = 16 / gcd(r, 16)
+            if (16 / g == 16 / C) return r;
+            r++;
+        }
+    }
+    // (double lines keep LP: their 16-byte accesses are served per
+    // quarter-warp, which the odd stride already spreads for C = 8)
+    static constexpr int ROWX = MODE == 0 || sizeof(T) != 4 ? LP : col_x();
+    // MODE 2 lands each input line in its own row of even stride (one
+    // 16-byte aligned bulk copy per line), read once before the exchange
     static constexpr int LPS = LP + (LP & 1);
-    static constexpr int ROW = MODE == 2 ? LPS : LP;
-    static constexpr int STAGE = ((C * ROW + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
+    static constexpr int ROWIN = MODE == 2 ? LPS : ROWX;
+    static constexpr int STAGE = ((C * (ROWIN > ROWX ? ROWIN : ROWX) + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
     static constexpr size_t PIPE_SMEM = 2 * (size_t)STAGE * sizeof(C2) + 16;
     static constexpr bool PIPE_OK = PIPE_SMEM <= 227 * 1024;
     // blocks per SM the register budget is sized for (about 24 warps)
@@ -397,11 +411,11 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
 #pragma unroll 1
             for (int r = 0; r < L; r += BR) tensor3d_g2s_hint(st + r * S::C, &tmap, col0 * XM, r, (int)ob, mb, pol);
         } else if (MODE == 2) {
-            // one row of stride ROW per line
+            // one row of stride ROWIN per line
             mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
 #pragma unroll 1
             for (int cc = 0; cc < lines; cc++)
-                bulk_g2s_hint(st + cc * S::ROW, in + line_off(p.lin, b0 + cc), (uint32_t)(L * ESZ), mb, pol);
+                bulk_g2s_hint(st + cc * S::ROWIN, in + line_off(p.lin, b0 + cc), (uint32_t)(L * ESZ), mb, pol);
         } else if (p.lin.inner == 1 && p.lin.outer == L) {
             // C consecutive contiguous rows: one copy
             mbar_arrive_expect_tx(mb, (uint32_t)(lines * L * ESZ));
@@ -463,10 +477,10 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             for (int m = 0; m < S::E; m++) v[m] = st[(t + m * S::TL) * S::C + c];
         } else {
 #pragma unroll
-            for (int m = 0; m < S::E; m++) v[m] = st[c * (MODE == 2 ? S::ROW : L) + t + m * S::TL];
+            for (int m = 0; m < S::E; m++) v[m] = st[c * (MODE == 2 ? S::ROWIN : L) + t + m * S::TL];
         }
         __syncthreads();  // every pass-0 read is done before the exchange writes
-        PadIdx xi{c * S::ROW};
+        PadIdx xi{c * S::ROWX};
         {
             C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
             const int j2 = tw ? (int)(b % p.tw_inner) : 0;
