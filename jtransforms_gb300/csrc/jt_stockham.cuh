@@ -59,7 +59,11 @@ template <typename T> struct StockCfg {
         return sizeof(T) == 4 ? (L <= 512 ? 16 : 8192 / L)
                               : (L <= 256 ? 8 : (4096 / L < 2 ? 2 : 4096 / L));
     }
-    static constexpr int C(int L, int mode) { return mode == 0 ? rows_C(L) : cols_C(L); }
+    // the transposing pass (MODE 2) at L <= 512 takes 8 lines: its half-
+    // warps then span two positions, so the 16-byte aligned input rows are
+    // read without bank conflicts (64-byte output segments)
+    static constexpr int rows2_C(int L) { return sizeof(T) == 4 && L <= 512 ? 8 : cols_C(L); }
+    static constexpr int C(int L, int mode) { return mode == 0 ? rows_C(L) : mode == 2 ? rows2_C(L) : cols_C(L); }
 };
 
 // Pass twiddle table of a length-L line (one per length, built by
