@@ -38,9 +38,9 @@ HEADLINE_SIZES = list(SIZES)
 # DRAM bytes (read + write) of one headline step, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, L2 kept between launches) of
 # the 256 MiB-per-size case, scaled by 4 (traffic grows with the transforms
-# processed): 2140 + 4071 + 3893 + 3932 + 6226 MB for 2^10 .. 2^24 (one pass,
+# processed): 2142 + 3996 + 3994 + 4044 + 6418 MB for 2^10 .. 2^24 (one pass,
 # two passes, two, two, three: each pass reads and writes the array)
-TRAFFIC_PER_STEP = 20.26e9
+TRAFFIC_PER_STEP = 20.59e9
 ELEMS = 2 ** 27          # complex elements per size per rank (1 GiB complex64)
 SEED = 20110602
 METRIC = "GFLOP/s (5N log2N) & % HBM roofline; TC-split vs plain FP32 at same error"
