@@ -457,6 +457,23 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         C2 *st = buf ? stage1 : stage0;
         const int64_t nxt = tile + gridDim.x;
         if (tid == 0 && nxt < ntiles) issue(nxt, buf ? stage0 : stage1, &bar[buf ^ 1]);
+        // Four-step twiddle w^{pos*j2} of this tile's outputs: the last pass
+        // writes pos = t + TL*m, so w^{pos*j2} = w^{t*j2} g^m with
+        // g = w^{TL*j2}.  Lines of 256+ take three table lookups, issued
+        // before the wait for the tile so their latency hides behind it
+        // (powers by products below); shorter tiles compute too briefly for
+        // that and look up seven factors at the store.
+        constexpr bool hoist = L >= 256;
+        typedef typename V2<T>::t C2T;
+        C2T tw_base, tw_g1, tw_g4;
+        if constexpr (tw && hoist) {
+            const int j2 = (int)((tile * S::C + c) % p.tw_inner);
+            const int g = S::TL * j2;
+            auto twv = [&](int x) { return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & lo_mask])); };
+            tw_base = twv(t * j2);
+            tw_g1 = twv(g);
+            tw_g4 = twv(4 * g);
+        }
         bool mine = mbar_wait_bounded(&bar[buf], (it >> 1) & 1, JT_MBAR_POLL_LIMIT);
         if (!__syncthreads_and(mine)) {
             ok = false;
@@ -487,28 +504,42 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         PadIdx xi{c * S::ROWX};
         {
             C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
-            const int j2 = tw ? (int)(b % p.tw_inner) : 0;
-            // Four-step twiddle w^{pos*j2}: the last pass writes pos = t + TL*m,
-            // m = q + k*NB for output slot q*R + k, so
-            // w^{pos*j2} = (w^{t*j2} w^{(m&3)*TL*j2}) * w^{(m>>2)*4*TL*j2}:
-            // seven table lookups per thread instead of one per output.
+            // output slot q*R + k holds pos = t + TL*m with m = q + k*NB:
+            // w^{pos*j2} = (base g^{m&3}) (g^4)^{m>>2}
             typedef typename S::template Pass<S::NPASS - 1> LP_;
-            auto twv = [&](int x) { return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & lo_mask])); };
+            const int j2 = tw && !hoist ? (int)(b % p.tw_inner) : 0;
             C2 bl[4], gh[4];
             auto store = [&](int pos, C2 val, int slot) {
                 if (tw) {
                     if (slot == 0) {
-                        const int g = S::TL * j2;
-                        C2 base = twv(t * j2);
-                        if (do_scale) base = cscale<T>(base, sc);  // the scale rides on the twiddle
-                        bl[0] = base;
-                        bl[1] = cmul<T>(base, twv(g));
-                        bl[2] = cmul<T>(base, twv(2 * g));
-                        bl[3] = cmul<T>(base, twv(3 * g));
-                        gh[0] = mk<T>(1, 0);
-                        gh[1] = twv(4 * g);
-                        gh[2] = twv(8 * g);
-                        gh[3] = twv(12 * g);
+                        if constexpr (hoist) {
+                            C2 base = tw_base;
+                            if (do_scale) base = cscale<T>(base, sc);  // the scale rides on the twiddle
+                            const C2 g2 = cmul<T>(tw_g1, tw_g1), g8 = cmul<T>(tw_g4, tw_g4);
+                            bl[0] = base;
+                            bl[1] = cmul<T>(base, tw_g1);
+                            bl[2] = cmul<T>(base, g2);
+                            bl[3] = cmul<T>(bl[2], tw_g1);
+                            gh[0] = mk<T>(1, 0);
+                            gh[1] = tw_g4;
+                            gh[2] = g8;
+                            gh[3] = cmul<T>(g8, tw_g4);
+                        } else {
+                            const int g = S::TL * j2;
+                            auto twv = [&](int x) {
+                                return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & lo_mask]));
+                            };
+                            C2 base = twv(t * j2);
+                            if (do_scale) base = cscale<T>(base, sc);
+                            bl[0] = base;
+                            bl[1] = cmul<T>(base, twv(g));
+                            bl[2] = cmul<T>(base, twv(2 * g));
+                            bl[3] = cmul<T>(base, twv(3 * g));
+                            gh[0] = mk<T>(1, 0);
+                            gh[1] = twv(4 * g);
+                            gh[2] = twv(8 * g);
+                            gh[3] = twv(12 * g);
+                        }
                     }
                     const int m = slot / LP_::R + (slot % LP_::R) * LP_::NB;
                     C2 w = m < 4 ? bl[m & 3] : cmul<T>(bl[m & 3], gh[m >> 2]);
