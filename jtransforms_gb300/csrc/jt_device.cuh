@@ -222,10 +222,29 @@ struct TileParams {
     int tw_lo_bits;
 };
 
+// b / d and b % d for the non-negative line indices of the kernels: shift and
+// mask for a power-of-two d (every power-of-two plan's layouts), 32-bit
+// division when both fit, 64-bit otherwise.
+__device__ __forceinline__ int64_t div_fast(int64_t b, int64_t d, int64_t *rem) {
+    if ((d & (d - 1)) == 0) {
+        *rem = b & (d - 1);
+        return b >> (__ffsll(d) - 1);
+    }
+    if (b <= 0x7fffffff && d <= 0x7fffffff) {
+        const uint32_t q = (uint32_t)b / (uint32_t)d;
+        *rem = b - (int64_t)q * d;
+        return q;
+    }
+    const int64_t q = b / d;
+    *rem = b - q * d;
+    return q;
+}
+
 __device__ __forceinline__ int64_t line_off(const Layout &l, int64_t b) {
     if (l.inner == 1) return b * l.outer;
-    int64_t q = b / l.inner;
-    return q * l.outer + (b - q * l.inner) * l.istride;
+    int64_t r;
+    const int64_t q = div_fast(b, l.inner, &r);
+    return q * l.outer + r * l.istride;
 }
 
 // One Stockham pass of radix R for every butterfly of the tile.

@@ -406,7 +406,8 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         const int lines = (int)min((int64_t)S::C, p.nlines - b0);
         if (MODE == 1) {
             // tile = C adjacent columns of one outer block
-            const int64_t ob = tl / p.tiles_per_col;
+            int64_t rem_unused;
+            const int64_t ob = div_fast(tl, p.tiles_per_col, &rem_unused);
             const int col0 = (int)((tl - ob * p.tiles_per_col) * S::C);
             constexpr int BR = L < 256 ? L : 256;
             constexpr int XM = sizeof(T) == 4 ? 1 : 2;  // f64 complex = two FLOAT64 in the map
@@ -467,7 +468,9 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         typedef typename V2<T>::t C2T;
         C2T tw_base, tw_g1, tw_g4;
         if constexpr (tw && hoist) {
-            const int j2 = (int)((tile * S::C + c) % p.tw_inner);
+            int64_t j2l;
+            div_fast(tile * S::C + c, p.tw_inner, &j2l);
+            const int j2 = (int)j2l;
             const int g = S::TL * j2;
             auto twv = [&](int x) { return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & lo_mask])); };
             tw_base = twv(t * j2);
@@ -507,7 +510,9 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             // output slot q*R + k holds pos = t + TL*m with m = q + k*NB:
             // w^{pos*j2} = (base g^{m&3}) (g^4)^{m>>2}
             typedef typename S::template Pass<S::NPASS - 1> LP_;
-            const int j2 = tw && !hoist ? (int)(b % p.tw_inner) : 0;
+            int64_t j2l = 0;
+            if (tw && !hoist) div_fast(b, p.tw_inner, &j2l);
+            const int j2 = (int)j2l;
             C2 bl[4], gh[4];
             auto store = [&](int pos, C2 val, int slot) {
                 if (tw) {
