@@ -123,6 +123,7 @@ def main(argv=None) -> int:
         results[lg] = {"best": key, "candidates": res}
         print(f"2^{lg}: best {key} {res[key]['GB/s']:.0f} GB/s", flush=True)
     out_dir = args.out_dir or os.path.join(HERE, "csrc")
+    os.makedirs(out_dir, exist_ok=True)
     write_header(best, os.path.join(out_dir, "jt_plan_table.h"))
     with open(os.path.join(args.out_dir or HERE, "plan_table_f32.json"), "w") as fh:
         json.dump({"device": torch.cuda.get_device_name(0), "mib_per_call": args.mib, "sizes": results}, fh, indent=1)

@@ -67,9 +67,11 @@ template <typename T> struct StockCfg {
 };
 
 // Pass twiddle table of a length-L line (one per length, built by
-// passtw_kernel): pass P >= 1 of radix R after NS = 16^P owns NS * R entries,
-// row jm holding w_{NS R}^{jm k} for k = 0..R-1, so the R - 1 factors a
-// butterfly needs are one contiguous, 16-byte aligned run.  Passes are
+// passtw_kernel): pass P >= 1 of radix R after NS = 16^P owns NS * R slots
+// holding w_{NS R}^{jm k} for jm < NS, k = 1..R-1, factor-major so that the
+// threads of a warp (consecutive jm) read consecutive addresses.  Float
+// tables: factor 1 as NS entries, then factors (2,3), (4,5), ... as NS
+// 16-byte pairs each; double tables: factor k as NS entries.  Passes are
 // radix 16 (E = 16 elements per thread) with a last pass of the remaining
 // radix.
 __host__ __device__ inline int stock_tw_count(int L) {
@@ -101,7 +103,18 @@ template <typename T> __global__ void passtw_kernel(typename V2<T>::t *out, int 
         const int R = P < nfull ? E : rem;
         if (P >= 1) {
             if (idx < off + ns * R) {
-                const int r = idx - off, jm = r / R, k = r - jm * R;
+                const int r = idx - off;
+                int jm, k;
+                if (sizeof(T) == 4) {
+                    // factor 1: slots [0, ns); pair p = (2p+2, 2p+3): ns pairs after that
+                    const int r2 = r - ns, pr = r2 / (2 * ns), rm = r2 - pr * 2 * ns;
+                    jm = r < ns ? r : rm >> 1;
+                    k = r < ns ? 1 : 2 * pr + 2 + (rm & 1);
+                } else {
+                    jm = r % ns;
+                    k = r / ns + 1;
+                }
+                if (k >= R) k = 0;  // the last ns slots are unused
                 const int64_t den = (int64_t)ns * R;
                 const int64_t num = ((int64_t)jm * k) % den;
                 double s, c;
@@ -193,29 +206,29 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
         if constexpr (P <= 1) return 0;
         else return twoff<P - 1>() + Pass<P - 1>::NS * Pass<P - 1>::R;
     }
-    // W: the pass twiddle table of length L.  Float rows are read two
-    // factors per 16-byte load.
+    // Factors w_{NS R}^{jm k}, k = 1..R-1, of pass P into tw[0..R-2], from
+    // the pass twiddle table W of length L (float pairs by 16-byte loads).
+    template <int P> static __device__ __forceinline__ void tw_row(int jm, const C2 *__restrict__ W, C2 *tw) {
+        typedef Pass<P> PP;
+        const C2 *base = W + twoff<P>();
+        if constexpr (sizeof(T) == 4) {
+            tw[0] = __ldg(base + jm);
+#pragma unroll
+            for (int p = 0; 2 * p + 2 < PP::R; p++) {
+                const float4 x = __ldg(reinterpret_cast<const float4 *>(base + PP::NS + 2 * p * PP::NS + 2 * jm));
+                tw[2 * p + 1] = make_float2(x.x, x.y);
+                tw[2 * p + 2] = make_float2(x.z, x.w);
+            }
+        } else {
+#pragma unroll
+            for (int k = 1; k < PP::R; k++) tw[k - 1] = __ldg(base + (k - 1) * PP::NS + jm);
+        }
+    }
     template <int P> static __device__ __forceinline__ void load_tw(int t, const C2 *__restrict__ W, C2 (&tw)[Tw<P>::N]) {
         typedef Pass<P> PP;
         if constexpr (PP::NS > 1) {
 #pragma unroll
-            for (int q = 0; q < PP::NB; q++) {
-                const int jm = (t + q * TL) & (PP::NS - 1);
-                const C2 *row = W + twoff<P>() + jm * PP::R;
-                if constexpr (sizeof(T) == 4) {
-                    // factor 1 alone, then factors (2,3), (4,5), ... in pairs
-                    tw[q * (PP::R - 1)] = __ldg(row + 1);
-#pragma unroll
-                    for (int k2 = 2; k2 < PP::R; k2 += 2) {
-                        const float4 x = __ldg(reinterpret_cast<const float4 *>(row + k2));
-                        tw[q * (PP::R - 1) + k2 - 1] = make_float2(x.x, x.y);
-                        tw[q * (PP::R - 1) + k2] = make_float2(x.z, x.w);
-                    }
-                } else {
-#pragma unroll
-                    for (int k = 1; k < PP::R; k++) tw[q * (PP::R - 1) + k - 1] = __ldg(row + k);
-                }
-            }
+            for (int q = 0; q < PP::NB; q++) tw_row<P>((t + q * TL) & (PP::NS - 1), W, &tw[q * (PP::R - 1)]);
         }
     }
 
@@ -553,7 +566,17 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
                 if (do_scale && !tw) val = cscale<T>(val, sc);
                 if (valid) st_hint(&dst[(int64_t)pos * oes32], val, spol);
             };
-            S::run_all(v, t, st, xi, W, store);
+            if constexpr (MODE == 0 && S::TL <= 32) {
+                // a warp holds whole lines: the exchanges need no CTA barrier
+                auto warp_sync = [] { __syncwarp(); };
+                S::run_all(v, t, st, xi, W, store, warp_sync);
+            } else if constexpr (MODE == 0 && S::C > 1 && S::C < 16) {
+                // a line spans TL / 32 warps: one named barrier per line
+                auto line_sync = [c] { named_barrier(1 + c, S::TL); };
+                S::run_all(v, t, st, xi, W, store, line_sync);
+            } else {
+                S::run_all(v, t, st, xi, W, store);
+            }
         }
         // this thread's generic writes to the stage come before the TMA that
         // refills it two tiles later

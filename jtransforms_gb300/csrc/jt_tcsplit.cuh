@@ -149,18 +149,13 @@ template <int L, int SIGN> struct TcPass {
             // first radix-16 pass -> second: output k of butterfly t is input
             // k' = 16 t / TL of butterfly j' = (16 t + k) mod TL of the next
             // pass (s = 0: idxD = 16 t), with factor w_256^{(j' mod 16) k'} =
-            // w_256^{k k'}: row k' of the pass-1 table (the table is symmetric)
+            // w_256^{k k'}: the pass-1 factors of jm = k' (the table is symmetric)
             static_assert(s == 0 && PP::NS == 1, "direct writes follow the first pass");
             const int kp = (16 * t) / K::TL;
             const int c = tid / K::TL;
-            const float4 *row = reinterpret_cast<const float4 *>(W + S::template twoff<1>() + kp * 16);
             float2 tw[16];
-#pragma unroll
-            for (int k2 = 0; k2 < 8; k2++) {
-                const float4 x = __ldg(row + k2);
-                tw[2 * k2] = make_float2(x.x, x.y);
-                tw[2 * k2 + 1] = make_float2(x.z, x.w);
-            }
+            tw[0] = make_float2(1.f, 0.f);
+            S::template tw_row<1>(kp, W, &tw[1]);
             const int colb = K::aoff(0, kp >> 1) + (kp & 1) * 8;  // chunk of column pair k', row 0
 #pragma unroll
             for (int k = 0; k < 16; k++) {
