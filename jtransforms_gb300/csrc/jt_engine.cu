@@ -82,6 +82,7 @@ struct Ctx {
     // depending on the previous step of the same transform
     std::vector<BOp> *rec = nullptr;
     int rec_prev = -1;
+    bool rec_sizing = false;  // the workspace-sizing pass before a recording
     // JT_MODE_TC_SPLIT: Float32 row passes of length 16..2048 run their
     // radix-16 stages on the tensor cores (jt_tcsplit.cuh)
     bool tc = false;
@@ -259,6 +260,9 @@ template <typename T> struct Fft1 {
     std::unique_ptr<Fft1> pc;
     C2 *Whi2 = nullptr, *Wlo2 = nullptr;  // four-step twiddle of length m
     int lo_bits2 = 0;
+    // batch recording of a one-pass length the batch kernel cannot hold
+    // (float lines of 8192+): the same transform in two passes
+    std::unique_ptr<Fft1> rec_alt;
     int64_t nB = 0;
     C2 *bk1 = nullptr, *bk2 = nullptr;
 
@@ -378,6 +382,14 @@ template <typename T> struct Fft1 {
             f->algo = ALG_TRIVIAL;
         } else if (sp && sp[0] == 0 && reg_ok(n)) {
             JT_TRY(f->init_direct());
+            if (!generic_ok(n) && !(sizeof(T) == 8 && n == 8192)) {
+                int lg = 0;
+                while (((int64_t)1 << lg) < n) lg++;
+                f->rec_alt.reset(new (std::nothrow) Fft1());
+                if (!f->rec_alt) return JT_ENOMEM;
+                f->rec_alt->n = n;
+                JT_TRY(f->rec_alt->init_twopass((int64_t)1 << (lg / 2)));
+            }
         } else if (sp && sp[0] > 0 && sp[2] == 0 && sp[0] <= 12 && sp[1] <= 12) {
             JT_TRY(f->init_twopass((int64_t)1 << sp[0]));
         } else if (sp && sp[2] > 0 && sizeof(T) == 4 && n <= ((int64_t)1 << 30) && sp[0] <= 12 && sp[1] <= 12 &&
@@ -623,6 +635,7 @@ template <typename T> struct Fft1 {
                 return JT_OK;
             }
             case ALG_DIRECT: {
+                if ((ctx.rec || ctx.rec_sizing) && rec_alt) return rec_alt->exec(ctx, in, din, out, dout, batch, sign, scale);
                 Layout li = {1, din, 0, 1}, lo = {1, dout, 0, 1};
                 return exec_direct(ctx, in, out, batch, li, lo, sign, scale);
             }
@@ -1725,6 +1738,7 @@ int batch_record(jt_batch *bt, std::vector<BOp> &ops, std::vector<std::vector<in
         Arena ar;
         Ctx c;
         c.dry = true;
+        c.rec_sizing = true;
         c.ws = &ar;
         std::lock_guard<std::mutex> g(im->mu);
         JT_TRY(im->run(c, bt->ops[i], (T *)bt->ptrs[i], 1, (ext + 1) & ~(int64_t)1, bt->scales[i] != 0));
