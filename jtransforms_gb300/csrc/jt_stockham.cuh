@@ -59,10 +59,14 @@ template <typename T> struct StockCfg {
         return sizeof(T) == 4 ? (L <= 512 ? 16 : 8192 / L)
                               : (L <= 256 ? 8 : (4096 / L < 2 ? 2 : 4096 / L));
     }
-    // the transposing pass (MODE 2) at L <= 512 takes 8 lines: its half-
-    // warps then span two positions, so the 16-byte aligned input rows are
-    // read without bank conflicts (64-byte output segments)
-    static constexpr int rows2_C(int L) { return sizeof(T) == 4 && L <= 512 ? 8 : cols_C(L); }
+    // the transposing pass (MODE 2) reads rows and stores from registers.
+    // At L <= 512 it takes 8 lines: its half-warps then span two positions,
+    // so the input rows are read without bank conflicts (64-byte output
+    // segments).  At 1024 it takes 4 (32-byte segments, which merge in L2):
+    // three CTAs per SM instead of one
+    static constexpr int rows2_C(int L) {
+        return sizeof(T) == 4 ? (L <= 512 ? 8 : L == 1024 ? 4 : cols_C(L)) : cols_C(L);
+    }
     static constexpr int C(int L, int mode) { return mode == 0 ? rows_C(L) : mode == 2 ? rows2_C(L) : cols_C(L); }
 };
 
@@ -178,15 +182,18 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     // quarter-warp, which the odd stride already spreads for C = 8)
     static constexpr int ROWX = MODE == 0 || sizeof(T) != 4 ? LP : col_x();
     // MODE 2 lands each input line in its own row of even stride (one
-    // 16-byte aligned bulk copy per line), read once before the exchange
+    // 16-byte aligned bulk copy per line), read once before the exchange:
+    // the exchange stride when that is even (C <= 8: its half-warps then
+    // read distinct banks), else the next even stride
     static constexpr int LPS = LP + (LP & 1);
-    static constexpr int ROWIN = MODE == 2 ? LPS : ROWX;
+    static constexpr int ROWIN = MODE == 2 ? (ROWX % 2 == 0 ? ROWX : LPS) : ROWX;
     static constexpr int STAGE = ((C * (ROWIN > ROWX ? ROWIN : ROWX) + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
     static constexpr size_t PIPE_SMEM = 2 * (size_t)STAGE * sizeof(C2) + 16;
     static constexpr bool PIPE_OK = PIPE_SMEM <= 227 * 1024;
     // blocks per SM the register budget is sized for (about 24 warps)
     // (double lines need twice the registers: no cap beyond one block at 256+)
-    static constexpr int MINB = sizeof(T) == 4 ? (NT >= 512 || NT < 64 ? 1 : 768 / NT)
+    // (single-warp blocks of short lines get more registers per thread: 18 warps)
+    static constexpr int MINB = sizeof(T) == 4 ? (NT >= 512 || NT < 32 ? 1 : NT < 64 ? 576 / NT : 768 / NT)
                                                : (NT >= 256 || NT < 64 ? 1 : 384 / NT);
 
     template <int P> struct Pass {
