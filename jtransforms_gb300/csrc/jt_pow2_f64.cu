@@ -8,7 +8,7 @@ namespace jt {
 bool stockham_pipe_ok(int L, int mode, const double *) {
 #define JT_PCASE(LL) \
     case LL:         \
-        return mode == 0 ? Stockham<double, LL, 0, -1>::PIPE_OK : (LL <= 4096 && Stockham<double, (LL <= 4096 ? LL : 16), 1, -1>::PIPE_OK);
+        return mode == 0 ? (Stockham<double, LL, 0, -1>::PIPE_OK || Stockham<double, LL, 0, -1>::BIG_OK) : (LL <= 4096 && Stockham<double, (LL <= 4096 ? LL : 16), 1, -1>::PIPE_OK);
     switch (L) {
         JT_PCASE(16) JT_PCASE(32) JT_PCASE(64) JT_PCASE(128) JT_PCASE(256) JT_PCASE(512) JT_PCASE(1024)
         JT_PCASE(2048) JT_PCASE(4096) JT_PCASE(8192)

@@ -190,6 +190,15 @@ template <typename T, int L, int MODE, int SIGN> struct Stockham {
     static constexpr int STAGE = ((C * (ROWIN > ROWX ? ROWIN : ROWX) + 15) / 16) * 16;  // keeps stage 1 128-byte aligned
     static constexpr size_t PIPE_SMEM = 2 * (size_t)STAGE * sizeof(C2) + 16;
     static constexpr bool PIPE_OK = PIPE_SMEM <= 227 * 1024;
+    // Row lines too long for two stages (stockham_big_kernel): one padded
+    // exchange line plus a stage for the first BIG_MP of the E element rows
+    // (m < BIG_MP of t + m*TL, a contiguous prefix of the line) of the next
+    // line; the thread reads the other rows from global memory.
+    static constexpr size_t BIG_X = ((size_t)LP * sizeof(C2) + 15) / 16 * 16;
+    static constexpr int BIG_MP_FIT = (int)((227 * 1024 - 16 - BIG_X) / ((size_t)TL * sizeof(C2)));
+    static constexpr int BIG_MP = BIG_MP_FIT > E ? E : BIG_MP_FIT;
+    static constexpr size_t BIG_SMEM = BIG_X + (size_t)BIG_MP * TL * sizeof(C2) + 16;
+    static constexpr bool BIG_OK = MODE == 0 && C == 1 && !PIPE_OK && BIG_MP >= E / 2;
     // blocks per SM the register budget is sized for (about 24 warps)
     // (double lines need twice the registers: no cap beyond one block at 256+)
     // (single-warp blocks of short lines get more registers per thread: 18 warps)
@@ -601,6 +610,76 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
     }
 }
 
+// Persistent row kernel for lines whose two-stage pipeline does not fit
+// (one line per CTA, a CTA of TL threads holds the whole line in
+// registers): the prefix of the next line comes in by one TMA bulk copy
+// into its own stage while the current line is computed in the exchange
+// line; the rest of the next line is read from global memory at the start
+// of its turn, issued before the wait for the copy.
+template <typename T, int L, int SIGN>
+__global__ void __launch_bounds__(Stockham<T, L, 0, SIGN>::NT, 1)
+    stockham_big_kernel(const typename V2<T>::t *in, typename V2<T>::t *out, StockParams p,
+                        const typename V2<T>::t *__restrict__ W, int *err) {
+    typedef Stockham<T, L, 0, SIGN> S;
+    typedef typename V2<T>::t C2;
+    constexpr int MP = S::BIG_MP;
+    constexpr uint32_t PBYTES = (uint32_t)(MP * S::TL * sizeof(C2));
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    C2 *xs = reinterpret_cast<C2 *>(smem_raw);
+    C2 *pst = reinterpret_cast<C2 *>(smem_raw + S::BIG_X);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + S::BIG_X + PBYTES);
+    const int t = threadIdx.x;
+    const int64_t ntiles = p.nlines;
+    const uint64_t pol = policy_evict_first();
+    const uint64_t spol = p.stream_out ? pol : policy_evict_normal();
+    auto issue = [&](int64_t tl) {
+        mbar_arrive_expect_tx(bar, PBYTES);
+        bulk_g2s_hint(pst, in + line_off(p.lin, tl), PBYTES, bar, pol);
+    };
+    if (t == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int64_t tile = blockIdx.x;
+    if (t == 0 && tile < ntiles) issue(tile);
+    const T sc = param_scale<T>(p);
+    const bool do_scale = p.do_scale != 0;
+    uint32_t it = 0;
+    bool ok = true;
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const C2 *src = in + line_off(p.lin, tile);
+        C2 v[S::E];
+#pragma unroll
+        for (int m = MP; m < S::E; m++) v[m] = src[t + m * S::TL];
+        const bool mine = mbar_wait_bounded(bar, it & 1, JT_MBAR_POLL_LIMIT);
+        if (!__syncthreads_and(mine)) {
+            ok = false;
+            break;
+        }
+#pragma unroll
+        for (int m = 0; m < MP; m++) v[m] = pst[t + m * S::TL];
+        // the stage's reads come before the copy that refills it
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (t == 0 && tile + gridDim.x < ntiles) issue(tile + gridDim.x);
+        C2 *dst = out + line_off(p.lout, tile);
+        auto store = [&](int pos, C2 val, int) {
+            if (do_scale) val = cscale<T>(val, sc);
+            st_hint(&dst[pos], val, spol);
+        };
+        PadIdx xi{0};
+        S::run_all(v, t, xs, xi, W, store);
+    }
+    if (!ok) {
+        if (t == 0) {
+            atomicExch(err, 1);
+            mbar_wait_bounded(bar, it & 1, JT_MBAR_POLL_LIMIT);  // the copy in flight
+        }
+        __syncthreads();
+    }
+}
+
 // Host-side launcher for one (T, L).
 template <typename T, int L> struct StockLaunch {
     typedef typename V2<T>::t C2;
@@ -634,6 +713,18 @@ template <typename T, int L> struct StockLaunch {
                                                   cudaStream_t s) {
         typedef Stockham<T, L, MODE, SIGN> S;
         int64_t ntiles = (p.nlines + S::C - 1) / S::C;
+        if constexpr (S::BIG_OK) if (tmap) {
+            auto kern = stockham_big_kernel<T, L, SIGN>;
+            static bool big_attr = false;
+            if (!big_attr) {
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BIG_SMEM);
+                cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+                big_attr = true;
+            }
+            const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms);
+            kern<<<(unsigned)grid, S::NT, S::BIG_SMEM, s>>>(in, out, p, W, err);
+            return;
+        }
         if constexpr (S::PIPE_OK) if (tmap) {
             if (MODE == 1 && p.tw_n != 0) pipe<MODE, SIGN, true>(in, out, p, *tmap, W, Whi, Wlo, err, sms, s, ntiles);
             else pipe<MODE, SIGN, false>(in, out, p, *tmap, W, Whi, Wlo, err, sms, s, ntiles);
