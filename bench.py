@@ -38,9 +38,9 @@ HEADLINE_SIZES = list(SIZES)
 # DRAM bytes (read + write) of one headline step, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, L2 kept between launches) of
 # the 256 MiB-per-size case, scaled by 4 (traffic grows with the transforms
-# processed): 2142 + 3996 + 3994 + 4044 + 6418 MB for 2^10 .. 2^24 (one pass,
-# two passes, two, two, three: each pass reads and writes the array)
-TRAFFIC_PER_STEP = 20.59e9
+# processed): 2145 + 2142 + 4040 + 4008 + 6158 MB for 2^10 .. 2^24 (one pass,
+# one, two, two, three: each pass reads and writes the array)
+TRAFFIC_PER_STEP = 18.49e9
 ELEMS = 2 ** 27          # complex elements per size per rank (1 GiB complex64)
 SEED = 20110602
 METRIC = "GFLOP/s (5N log2N) & % HBM roofline; TC-split vs plain FP32 at same error"
@@ -585,8 +585,8 @@ def run_ours(args, world, rank, local):
                          "traffic": TRAFFIC_PER_STEP * (ELEMS / 2 ** 27) if SIZES == HEADLINE_SIZES else None,
                          "traffic_unit": "bytes per step (DRAM read + write of the five calls)",
                          "peak_source": peak_src,
-                         "kernel": "stockham_pipe_kernel (every launch of the five 1 GiB calls: one pass at 2^10, "
-                                   "passes A and B at 2^14..2^24)",
+                         "kernel": "stockham_pipe_kernel / stockham_big_kernel (every launch of the five 1 GiB "
+                                   "calls: one pass at 2^10 and 2^14, passes A and B at 2^18..2^24)",
                          "algorithmic_bytes_per_call": 2 * 8 * ELEMS,
                          "algorithmic_bytes_per_step": bytes_step},
             "per_size": per_size, "rel_l2_vs_fp64": err, "rel_l2_vs_fp64_set_b": err_b,
