@@ -158,16 +158,17 @@ int jt_batch_destroy(jt_batch *batch);
                                      1..16384); the intermediate scratch is one chunk */
 #define JT_OPT_HOST_PIECE_MB 6   /* MiB per piece of a host-array batch (default 64, 1..16384):
                                     pieces are copied in, transformed and copied out overlapped */
-#define JT_OPT_THREEPASS_MIN_LOG2 5 /* float powers of two from 2^value (up to 2^30) use three
-                                       passes of near-equal lengths (default 21; 0: never).  Read
-                                       when a plan is created. */
+#define JT_OPT_THREEPASS_MIN_LOG2 5 /* float powers of two from 2^value use three passes of
+                                       near-equal lengths (default 21; 0: only beyond 2^24, where
+                                       every power of two up to 2^32 takes three).  Read when a
+                                       plan is created. */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 
 /* Pass split of power-of-two length 2^log2n in `prec` for plans created from
  * now on, overriding the compiled plan table (the autotuner's probe):
  * (0,0,0) one pass; (a,b,0) two passes 2^a x 2^b, a + b = log2n, each <= 12;
- * (a,b,c) three passes (Float32 only), a + b + c = log2n; a < 0 clears the
+ * (a,b,c) three passes, a + b + c = log2n; a < 0 clears the
  * override.  No counterpart in the reference. */
 int jt_set_split(int prec, int log2n, int a, int b, int c);
 

@@ -218,6 +218,10 @@ static bool make_col_tmap(CUtensorMap *m, const void *base, int esz, int64_t inn
 // Complex FFT of one length
 // ---------------------------------------------------------------------------
 enum { ALG_DIRECT = 0, ALG_TWOPASS = 1, ALG_BLUESTEIN = 2, ALG_TRIVIAL = 3, ALG_THREEPASS = 4 };
+// longest power-of-two line of the multi-pass register plans: twiddle
+// exponents are formed in 32 bits modulo the length (three passes of up to
+// 2048 reach it)
+static constexpr int64_t kPow2PassMax = (int64_t)1 << 32;
 
 static const int kMaxThreads = 512;
 
@@ -392,16 +396,17 @@ template <typename T> struct Fft1 {
             }
         } else if (sp && sp[0] > 0 && sp[2] == 0 && sp[0] <= 12 && sp[1] <= 12) {
             JT_TRY(f->init_twopass((int64_t)1 << sp[0]));
-        } else if (sp && sp[2] > 0 && sizeof(T) == 4 && n <= ((int64_t)1 << 30) && sp[0] <= 12 && sp[1] <= 12 &&
-                   sp[2] <= 12) {  // twiddle exponents stay below 2^31
+        } else if (sp && sp[2] > 0 && n <= kPow2PassMax && sp[0] <= 12 && sp[1] <= 12 && sp[2] <= 12) {
             JT_TRY(f->init_threepass((int64_t)1 << sp[0], (int64_t)1 << sp[1], (int64_t)1 << sp[2]));
         } else if (direct_ok(n) && (!is_pow2(n) || n <= one_pass_max())) {
             JT_TRY(f->init_direct());
-        } else if (sizeof(T) == 4 && is_pow2(n) && g_opt_threepass_min.load() > 0 && n >= g_opt_threepass_min.load() &&
-                   n <= ((int64_t)1 << 30)) {
+        } else if (is_pow2(n) && n <= kPow2PassMax &&
+                   ((sizeof(T) == 4 && g_opt_threepass_min.load() > 0 && n >= g_opt_threepass_min.load()) ||
+                    n > (int64_t)4096 * 4096)) {
             // three register-kernel passes of lengths as equal as possible
             // (2^24 = 256^3): every pass runs 128-byte-wide column tiles,
-            // where a 4096 x 4096 split would run 16-byte ones
+            // where a 4096 x 4096 split would run 16-byte ones; beyond
+            // 4096 x 4096 three passes are the only register-kernel split
             int lg = 0;
             while (((int64_t)1 << lg) < n) lg++;
             const int a = lg / 3, b = (lg - a) / 2, c = lg - a - b;
@@ -426,7 +431,7 @@ template <typename T> struct Fft1 {
             } else {
                 f->algo = ALG_BLUESTEIN;
                 f->nB = next_pow2(2 * n - 1);
-                if (f->nB > Lim<T>::lmax() * Lim<T>::lmax()) return JT_ETOOBIG;
+                if (f->nB > kPow2PassMax) return JT_ETOOBIG;
                 JT_TRY(create(f->nB, f->pbl));
                 JT_TRY(f->make_chirp());
             }
@@ -521,6 +526,10 @@ template <typename T> struct Fft1 {
             sp.tw_n = tw_n;
             sp.tw_inner = tw_inner;
             sp.tw_lo_bits = tw_lo_bits;
+            // register kernels form twiddle exponents in 32 bits, reduced
+            // modulo a power-of-two tw_n (up to 2^32); other lengths below 2^31
+            if (tw_n != 0 && (is_pow2(tw_n) ? tw_n > ((int64_t)1 << 32) : tw_n >= ((int64_t)1 << 31))) return JT_ETOOBIG;
+            sp.tw_mask = tw_n != 0 && is_pow2(tw_n) ? (uint32_t)(tw_n - 1) : 0xffffffffu;
             sp.discard_in = hint_discard_in;
             sp.stream_out = hint_stream_out;
             if (ctx.dry) return JT_OK;
@@ -1657,7 +1666,7 @@ int jt_set_split(int prec, int log2n, int a, int b, int c) {
     }
     const bool one = a == 0 && b == 0 && c == 0;
     const bool two = a >= 1 && b >= 1 && c == 0 && a <= 12 && b <= 12 && a + b == log2n;
-    const bool three = prec == JT_FLOAT32 && a >= 1 && b >= 1 && c >= 1 && a <= 12 && b <= 12 && c <= 12 && a + b + c == log2n;
+    const bool three = a >= 1 && b >= 1 && c >= 1 && a <= 12 && b <= 12 && c <= 12 && a + b + c == log2n;
     if (!one && !two && !three) return JT_EINVAL;
     e[0] = (signed char)a;
     e[1] = (signed char)b;

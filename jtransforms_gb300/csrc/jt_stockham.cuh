@@ -40,10 +40,22 @@ struct StockParams {
     int do_scale;
     int64_t tw_n, tw_inner;  // four-step output twiddle w_{tw_n}^{pos * (b % tw_inner)}; tw_n = 0: none
     int tw_lo_bits;
+    uint32_t tw_mask;        // exponent reduction: tw_n - 1 for a power of two up to 2^32, else all ones
     int64_t tiles_per_col;   // MODE 1 pipe: column tiles per outer block (inner / C)
     int discard_in;          // MODE 2 pipe: the input is a dead intermediate (drop it from L2)
     int stream_out;          // outputs are not re-read soon: streaming stores
 };
+
+// w_{tw_n}^x from the two-level table.  x is formed in 32-bit unsigned
+// arithmetic: for a power-of-two tw_n up to 2^32 the wrap keeps x mod tw_n
+// and the mask finishes the reduction; other lengths stay below 2^31.
+template <typename T>
+__device__ __forceinline__ typename V2<T>::t tw_lookup(const typename V2<T>::t *__restrict__ Whi,
+                                                      const typename V2<T>::t *__restrict__ Wlo, uint32_t x,
+                                                      const StockParams &p) {
+    x &= p.tw_mask;
+    return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & ((1u << p.tw_lo_bits) - 1u)]));
+}
 
 template <typename T> __device__ __forceinline__ T param_scale(const StockParams &p) {
     if constexpr (sizeof(T) == 4) return p.scalef;
@@ -369,14 +381,12 @@ __device__ void stockham_body(const typename V2<T>::t *__restrict__ in, typename
     C2 *dst = out + (valid ? line_off(p.lout, b) : 0);
     const int oes32 = MODE == 0 ? 1 : (int)p.lout.estride;
     const bool tw = p.tw_n != 0;
-    const int j2 = tw ? (int)(b % p.tw_inner) : 0;
-    const int lo_mask = (1 << p.tw_lo_bits) - 1;
+    const uint32_t j2 = tw ? (uint32_t)(b % p.tw_inner) : 0u;
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
     auto store = [&](int pos, C2 val, int) {
         if (tw) {
-            const int tt = pos * j2;  // < tw_n <= 2^26
-            C2 w = cmul<T>(__ldg(&Whi[tt >> p.tw_lo_bits]), __ldg(&Wlo[tt & lo_mask]));
+            C2 w = tw_lookup<T>(Whi, Wlo, (uint32_t)pos * j2, p);
             val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
         }
         if (do_scale) val = cscale<T>(val, sc);
@@ -475,7 +485,6 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
     // the four-step twiddle belongs to the column pass (the launcher picks
     // the TW variant from tw_n)
     constexpr bool tw = MODE == 1 && TW;
-    const int lo_mask = (1 << p.tw_lo_bits) - 1;
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
     const int oes32 = MODE == 0 ? 1 : (int)p.lout.estride;
@@ -499,12 +508,11 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         if constexpr (tw && hoist) {
             int64_t j2l;
             div_fast(tile * S::C + c, p.tw_inner, &j2l);
-            const int j2 = (int)j2l;
-            const int g = S::TL * j2;
-            auto twv = [&](int x) { return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & lo_mask])); };
-            tw_base = twv(t * j2);
-            tw_g1 = twv(g);
-            tw_g4 = twv(4 * g);
+            const uint32_t j2 = (uint32_t)j2l;
+            const uint32_t g = (uint32_t)S::TL * j2;
+            tw_base = tw_lookup<T>(Whi, Wlo, (uint32_t)t * j2, p);
+            tw_g1 = tw_lookup<T>(Whi, Wlo, g, p);
+            tw_g4 = tw_lookup<T>(Whi, Wlo, 4u * g, p);
         }
         bool mine = mbar_wait_bounded(&bar[buf], (it >> 1) & 1, JT_MBAR_POLL_LIMIT);
         if (!__syncthreads_and(mine)) {
@@ -541,7 +549,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             typedef typename S::template Pass<S::NPASS - 1> LP_;
             int64_t j2l = 0;
             if (tw && !hoist) div_fast(b, p.tw_inner, &j2l);
-            const int j2 = (int)j2l;
+            const uint32_t j2 = (uint32_t)j2l;
             C2 bl[4], gh[4];
             auto store = [&](int pos, C2 val, int slot) {
                 if (tw) {
@@ -559,20 +567,18 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
                             gh[2] = g8;
                             gh[3] = cmul<T>(g8, tw_g4);
                         } else {
-                            const int g = S::TL * j2;
-                            auto twv = [&](int x) {
-                                return cmul<T>(__ldg(&Whi[x >> p.tw_lo_bits]), __ldg(&Wlo[x & lo_mask]));
-                            };
-                            C2 base = twv(t * j2);
+                            const uint32_t g = (uint32_t)S::TL * j2;
+                            auto twv = [&](uint32_t x) { return tw_lookup<T>(Whi, Wlo, x, p); };
+                            C2 base = twv((uint32_t)t * j2);
                             if (do_scale) base = cscale<T>(base, sc);
                             bl[0] = base;
                             bl[1] = cmul<T>(base, twv(g));
-                            bl[2] = cmul<T>(base, twv(2 * g));
-                            bl[3] = cmul<T>(base, twv(3 * g));
+                            bl[2] = cmul<T>(base, twv(2u * g));
+                            bl[3] = cmul<T>(base, twv(3u * g));
                             gh[0] = mk<T>(1, 0);
-                            gh[1] = twv(4 * g);
-                            gh[2] = twv(8 * g);
-                            gh[3] = twv(12 * g);
+                            gh[1] = twv(4u * g);
+                            gh[2] = twv(8u * g);
+                            gh[3] = twv(12u * g);
                         }
                     }
                     const int m = slot / LP_::R + (slot % LP_::R) * LP_::NB;
@@ -884,8 +890,7 @@ __global__ void __launch_bounds__(ColPass<T, L, MODE, SIGN>::NT, ColPass<T, L, M
     constexpr int NSL = S::template Pass<S::NPASS - 1>::NS;
     if (MODE == 2) __syncthreads();  // every row is read: the tile may be overwritten
     const bool tw = p.tw_n != 0;
-    const int j2 = x0 + c;
-    const int lo_mask = (1 << p.tw_lo_bits) - 1;
+    const uint32_t j2 = (uint32_t)(x0 + c);
     const T sc = param_scale<T>(p);
     const bool do_scale = p.do_scale != 0;
 #pragma unroll
@@ -895,8 +900,7 @@ __global__ void __launch_bounds__(ColPass<T, L, MODE, SIGN>::NT, ColPass<T, L, M
             const int pos = t + q * CP::TL + k * NSL;
             C2 val = o[q * RL + k];
             if (tw) {
-                const int tt = pos * j2;
-                C2 w = cmul<T>(__ldg(&Whi[tt >> p.tw_lo_bits]), __ldg(&Wlo[tt & lo_mask]));
+                C2 w = tw_lookup<T>(Whi, Wlo, (uint32_t)pos * j2, p);
                 val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
             }
             if (do_scale) val = cscale<T>(val, sc);

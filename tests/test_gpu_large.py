@@ -66,7 +66,7 @@ def test_set_split_rules():
     lib = N.load()
     assert lib.jt_set_split(N.FLOAT32, 20, 10, 9, 0) == N.EINVAL      # sums to 19
     assert lib.jt_set_split(N.FLOAT32, 26, 13, 13, 0) == N.EINVAL     # a pass above 4096
-    assert lib.jt_set_split(N.FLOAT64, 24, 8, 8, 8) == N.EINVAL       # three passes: Float32 only
+    assert lib.jt_set_split(N.FLOAT64, 24, 13, 6, 5) == N.EINVAL      # a pass above 4096
     assert lib.jt_set_split(N.FLOAT32, 31, 0, 0, 0) == N.EINVAL
 
 
