@@ -104,3 +104,21 @@ def test_config_setters_are_accepted():
     assert J.ConcurrencyUtils.getNumberOfThreads() == 4
     assert J.CommonUtils.getReminder(10158) == 1693
     assert J.CommonUtils.nextPow2(2 * 10158 - 1) == 32768
+
+
+def test_split_override_rules(lib):
+    """jt_set_split (host logic only): one, two or three passes of at most
+    4096 each summing to log2 n, for both precisions; anything else is
+    refused and a negative first length clears the override."""
+    from jtransforms_gb300 import _native as N
+    try:
+        assert lib.jt_set_split(N.FLOAT32, 20, 10, 10, 0) == N.OK
+        assert lib.jt_set_split(N.FLOAT64, 26, 9, 9, 8) == N.OK       # three passes in double too
+        assert lib.jt_set_split(N.FLOAT64, 14, 0, 0, 0) == N.OK
+        assert lib.jt_set_split(N.FLOAT32, 20, 10, 9, 0) == N.EINVAL  # sums to 19
+        assert lib.jt_set_split(N.FLOAT32, 26, 13, 13, 0) == N.EINVAL  # a pass above 4096
+        assert lib.jt_set_split(N.FLOAT64, 24, 13, 6, 5) == N.EINVAL
+        assert lib.jt_set_split(2, 20, 10, 10, 0) == N.EINVAL          # no such precision
+    finally:
+        for prec, lg in ((N.FLOAT32, 20), (N.FLOAT64, 26), (N.FLOAT64, 14)):
+            assert lib.jt_set_split(prec, lg, -1, 0, 0) == N.OK
