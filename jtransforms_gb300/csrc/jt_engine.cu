@@ -506,7 +506,7 @@ template <typename T> struct Fft1 {
     // DIRECT pass over `nlines` lines with arbitrary layouts.
     int exec_direct(Ctx &ctx, const C2 *in, C2 *out, int64_t nlines, const Layout &lin, const Layout &lout, int sign,
                     double scale, int64_t tw_n = 0, int64_t tw_inner = 1, const C2 *Whi_ = nullptr, const C2 *Wlo_ = nullptr,
-                    int tw_lo_bits = 0, int hint_discard_in = 0, int hint_stream_out = 1) const {
+                    int tw_lo_bits = 0, int hint_discard_in = 0, int hint_stream_out = 1, int hint_reverse = 0) const {
         if (nlines <= 0) return JT_OK;
         if (ctx.rec) return record_lines(ctx, in, out, nlines, lin, lout, sign, scale, tw_n, tw_inner, Whi_, Wlo_, tw_lo_bits);
         if (reg) {
@@ -532,6 +532,7 @@ template <typename T> struct Fft1 {
             sp.tw_mask = tw_n != 0 && is_pow2(tw_n) ? (uint32_t)(tw_n - 1) : 0xffffffffu;
             sp.discard_in = hint_discard_in;
             sp.stream_out = hint_stream_out;
+            sp.reverse = hint_reverse;
             if (ctx.dry) return JT_OK;
             const int esz = (int)sizeof(C2);
             // split-operand tensor-core kernel for Float32 row passes
@@ -657,7 +658,10 @@ template <typename T> struct Fft1 {
                     Layout lai = {n2, din, 1, n2}, lao = {n2, n, 1, n2};
                     JT_TRY(pa->exec_direct(ctx, in + b * din, tmp, cb * n2, lai, lao, sign, 1.0, n, n2, Whi, Wlo, lo_bits, 0, 0));
                     Layout lbi = {n1, n, n2, 1}, lbo = {n1, dout, 1, n1};
-                    JT_TRY(pb->exec_direct(ctx, tmp, out + b * dout, cb * n1, lbi, lbo, sign, scale, 0, 1, nullptr, nullptr, 0, 1, 1));
+                    // pass B walks its tiles last to first: the transforms
+                    // pass A wrote last are still in L2
+                    JT_TRY(pb->exec_direct(ctx, tmp, out + b * dout, cb * n1, lbi, lbo, sign, scale, 0, 1, nullptr, nullptr, 0, 1, 1,
+                                           1));
                 }
                 return JT_OK;
             }

@@ -44,6 +44,7 @@ struct StockParams {
     int64_t tiles_per_col;   // MODE 1 pipe: column tiles per outer block (inner / C)
     int discard_in;          // MODE 2 pipe: the input is a dead intermediate (drop it from L2)
     int stream_out;          // outputs are not re-read soon: streaming stores
+    int reverse;             // pipe: walk the tiles last to first (the input's freshest part is in L2)
 };
 
 // w_{tw_n}^x from the two-level table.  x is formed in 32-bit unsigned
@@ -479,8 +480,12 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         if (MODE == 1) prefetch_tensormap(&tmap);
     }
     __syncthreads();
+    // tile schedule index -> tile: a pass reading what the previous pass
+    // just wrote starts with its last tiles, still in L2
+    const bool rev = p.reverse != 0;
+    auto act = [&](int64_t x) -> int64_t { return rev ? ntiles - 1 - x : x; };
     int64_t tile = blockIdx.x;
-    if (tid == 0 && tile < ntiles) issue(tile, stage0, &bar[0]);
+    if (tid == 0 && tile < ntiles) issue(act(tile), stage0, &bar[0]);
 
     // the four-step twiddle belongs to the column pass (the launcher picks
     // the TW variant from tw_n)
@@ -495,7 +500,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         const int buf = it & 1;
         C2 *st = buf ? stage1 : stage0;
         const int64_t nxt = tile + gridDim.x;
-        if (tid == 0 && nxt < ntiles) issue(nxt, buf ? stage0 : stage1, &bar[buf ^ 1]);
+        if (tid == 0 && nxt < ntiles) issue(act(nxt), buf ? stage0 : stage1, &bar[buf ^ 1]);
         // Four-step twiddle w^{pos*j2} of this tile's outputs: the last pass
         // writes pos = t + TL*m, so w^{pos*j2} = w^{t*j2} g^m with
         // g = w^{TL*j2}.  Lines of 256+ take three table lookups, issued
@@ -507,7 +512,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
         C2T tw_base, tw_g1, tw_g4;
         if constexpr (tw && hoist) {
             int64_t j2l;
-            div_fast(tile * S::C + c, p.tw_inner, &j2l);
+            div_fast(act(tile) * S::C + c, p.tw_inner, &j2l);
             const uint32_t j2 = (uint32_t)j2l;
             const uint32_t g = (uint32_t)S::TL * j2;
             tw_base = tw_lookup<T>(Whi, Wlo, (uint32_t)t * j2, p);
@@ -519,7 +524,7 @@ __global__ void __launch_bounds__(Stockham<T, L, MODE, SIGN>::NT, Stockham<T, L,
             ok = false;
             break;
         }
-        const int64_t b0 = tile * S::C;
+        const int64_t b0 = act(tile) * S::C;
         const int64_t b = b0 + c;
         // column tiles are whole (the launcher requires nlines % C == 0)
         const bool valid = MODE == 1 || b < p.nlines;

@@ -167,3 +167,33 @@ def test_round_trips(n):
     f.realForward(r)
     f.realInverse(r, True)
     assert rmse(r, x[:n]) < 1e-12
+
+
+@pytest.mark.parametrize("prec,n", [("f32", 8192), ("f32", 16384), ("f64", 4096), ("f64", 8192)])
+@pytest.mark.parametrize("gap", [0, 8, 2])
+def test_long_lines_batched_with_gaps(prec, n, gap):
+    """The one-pass kernels of the longest lines (the two-stage pipeline at
+    float 8192 and double 4096, the prefix-prefetch kernel at float 16384
+    and double 8192) over a device batch whose arrays sit `gap` elements
+    apart: 0 and 8 keep TMA's 16-byte rules (contiguous lines, strided
+    lines); 2 floats break them (the plain kernel); against an FP64 FFT."""
+    import torch
+    from jtransforms_gb300 import _native as N
+    if prec == "f64" and gap == 2:
+        pytest.skip("a double complex line is 16-byte aligned at every even gap")
+    dt, _ = _classes()[prec]
+    f = _plan(prec, n)
+    batch, ext = 5, 2 * n
+    dist = ext + gap
+    rng = np.random.default_rng(n + gap)
+    host = rng.uniform(-1, 1, dist * batch).astype(dt)
+    dev = torch.from_numpy(host.copy()).cuda()
+    f.plan.execute(N.COMPLEX_FORWARD, dev, 0, False, batch=batch, dist=dist)
+    got = dev.cpu().numpy()
+    for b in range(batch):
+        z = host[b * dist:b * dist + ext].astype(np.float64)
+        y = np.fft.fft(z[0::2] + 1j * z[1::2])
+        want = np.empty(ext)
+        want[0::2], want[1::2] = y.real, y.imag
+        assert rel_l2(got[b * dist:b * dist + ext], want) <= tol(n, dt)
+        assert np.array_equal(got[b * dist + ext:(b + 1) * dist], host[b * dist + ext:(b + 1) * dist])
