@@ -38,9 +38,9 @@ HEADLINE_SIZES = list(SIZES)
 # DRAM bytes (read + write) of one headline step, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, L2 kept between launches) of
 # the 256 MiB-per-size case, scaled by 4 (traffic grows with the transforms
-# processed): 2145 + 2142 + 4040 + 4008 + 6158 MB for 2^10 .. 2^24 (one pass,
+# processed): 2144 + 2142 + 3827 + 3789 + 6310 MB for 2^10 .. 2^24 (one pass,
 # one, two, two, three: each pass reads and writes the array)
-TRAFFIC_PER_STEP = 18.49e9
+TRAFFIC_PER_STEP = 18.21e9
 ELEMS = 2 ** 27          # complex elements per size per rank (1 GiB complex64)
 SEED = 20110602
 METRIC = "GFLOP/s (5N log2N) & % HBM roofline; TC-split vs plain FP32 at same error"
