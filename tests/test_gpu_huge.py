@@ -12,7 +12,7 @@ at :122), where n = 2^31 complex floats is 2^32 array elements.
     elsewhere;
   - forward then scaled inverse returns the input.
 
-Tolerance: relative L2 <= 4 * eps * log2(n), the benchmark spec bound.
+Tolerance: relative L2 <= 4 * eps * log2(n) of the precision.
 """
 import math
 

@@ -2,7 +2,7 @@
 table's choice (two or three passes) and every split kind forced through
 jt_set_split, against an FP64 FFT of the same input; realForward of a length
 whose half-length FFT runs three passes.  Tolerance: relative L2 <=
-4 * eps_float * log2(n) against FP64 (the benchmark spec bound)."""
+4 * eps_float * log2(n) against FP64."""
 import numpy as np
 import pytest
 
