@@ -467,8 +467,6 @@ def run_ours(args, world, rank, local):
         N.set_option(N.OPT_TMA_PIPELINE, 0)
     if args.direct_max:
         N.set_option(N.OPT_DIRECT_MAX_F32, args.direct_max)
-    if args.no_colpass:
-        N.set_option(N.OPT_COLUMN_KERNEL, 0)
     if args.chunk_mb:
         N.set_option(N.OPT_TWOPASS_CHUNK_MB, args.chunk_mb)
     if args.host_piece_mb:
@@ -634,7 +632,6 @@ def main():
     ap.add_argument("--sizes", type=str, default="", help="comma-separated subset of the headline sizes")
     ap.add_argument("--no-tma", action="store_true", help="use the plain (non-TMA) power-of-two kernel")
     ap.add_argument("--direct-max", type=int, default=0, help="longest float length done in one pass")
-    ap.add_argument("--no-colpass", action="store_true", help="column passes on the tile-pipelined kernel")
     ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 1024)")
     ap.add_argument("--host-piece-mb", type=int, default=0, help="MiB per piece of the end-to-end host batch (library default 64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")

@@ -152,8 +152,8 @@ int jt_batch_destroy(jt_batch *batch);
 #define JT_OPT_DIRECT_MAX_F32 1 /* longest power-of-two float length done in one pass (default 8192);
                                    longer lengths use two passes.  Read when a plan is created. */
 #define JT_OPT_DIRECT_MAX_F64 2 /* the same for double (default 8192) */
-#define JT_OPT_COLUMN_KERNEL 3  /* 0 (default): column passes use the tile-pipelined kernel; 1: the
-                                   line-group kernel with swizzled TMA tensor loads and stores */
+#define JT_OPT_COLUMN_KERNEL 3  /* 0 only: column passes use the tile-pipelined kernel (other values
+                                   return JT_EINVAL) */
 #define JT_OPT_TWOPASS_CHUNK_MB 4 /* MiB of transforms per two-pass chunk and launch (default 1024,
                                      1..16384); the intermediate scratch is one chunk */
 #define JT_OPT_HOST_PIECE_MB 6   /* MiB per piece of a host-array batch (default 64, 1..16384):

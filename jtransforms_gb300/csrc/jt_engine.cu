@@ -128,7 +128,6 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 static EncodeTiledFn g_encode_tiled = nullptr;
 static std::atomic<int> g_opt_tma{1};
-static std::atomic<int> g_opt_colpass{0};
 static std::atomic<int> g_opt_direct_max_f32{8192};
 static std::atomic<int> g_opt_direct_max_f64{8192};
 static std::atomic<int> g_opt_chunk_mb{1024};
@@ -183,20 +182,14 @@ bool stockham_pipe_ok(int L, int mode, const float *);
 bool stockham_pipe_ok(int L, int mode, const double *);
 int stockham_lines_per_cta(int L, int mode, const float *);
 int stockham_lines_per_cta(int L, int mode, const double *);
-bool colpass_cfg(int L, int mode, int *C, int *swb, const float *);
-bool colpass_cfg(int L, int mode, int *C, int *swb, const double *);
-bool colpass_launch(int L, int mode, int sign, const float2 *in, const StockParams &p, const CUtensorMap &tin,
-                    const CUtensorMap &tout, const float2 *W, const float2 *Whi, const float2 *Wlo, int *err, cudaStream_t s);
 bool tc_split_ok(int L);
 bool tc_split_launch(int L, int sign, const float2 *in, float2 *out, const StockParams &p, const float2 *W, int *err, int sms,
                      cudaStream_t s);
-bool colpass_launch(int L, int mode, int sign, const double2 *in, const StockParams &p, const CUtensorMap &tin,
-                    const CUtensorMap &tout, const double2 *W, const double2 *Whi, const double2 *Wlo, int *err, cudaStream_t s);
 
 // Encodes a 3D tiled tensor map over complex elements of esz bytes (8 or 16,
 // moved as 8-byte units): x = column (inner), y = row, z = outer block.
 static bool make_col_tmap(CUtensorMap *m, const void *base, int esz, int64_t inner, int64_t rows, int64_t nblocks,
-                          int64_t row_pitch, int64_t block_stride, int C, int BR, int swb = 0) {
+                          int64_t row_pitch, int64_t block_stride, int C, int BR) {
     if (!g_encode_tiled) return false;
     const int xm = esz / 8;
     cuuint64_t dims[3] = {(cuuint64_t)(inner * xm), (cuuint64_t)rows, (cuuint64_t)nblocks};
@@ -205,12 +198,7 @@ static bool make_col_tmap(CUtensorMap *m, const void *base, int esz, int64_t inn
     cuuint32_t es[3] = {1, 1, 1};
     if ((row_pitch * esz) % 16 || (block_stride * esz) % 16 || ((uintptr_t)base % 16)) return false;
     return g_encode_tiled(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(base), dims, strides, box, es,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          swb == 3 ? CU_TENSOR_MAP_SWIZZLE_128B
-                          : swb == 2 ? CU_TENSOR_MAP_SWIZZLE_64B
-                          : swb == 1 ? CU_TENSOR_MAP_SWIZZLE_32B
-                                     : CU_TENSOR_MAP_SWIZZLE_NONE,
-                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -543,30 +531,6 @@ template <typename T> struct Fft1 {
                         return JT_ECUDA;
                     g_launches++;
                     return JT_OK;
-                }
-            }
-            // column passes: group-per-line kernel with TMA tensor load/store
-            if ((mode == 1 || mode == 2) && g_opt_tma.load() && g_opt_colpass.load()) {
-                int Cc = 0, swb = 0;
-                if (colpass_cfg((int)n, mode, &Cc, &swb, (const T *)nullptr) && ((uintptr_t)out % 16) == 0 &&
-                    lout.istride == 1 && lout.inner % Cc == 0 && nlines % lout.inner == 0 && nlines % Cc == 0) {
-                    CUtensorMap tin, tout;
-                    memset(&tin, 0, sizeof(tin));
-                    const int BR = (int)std::min<int64_t>(n, 256);
-                    bool ok = make_col_tmap(&tout, out, esz, lout.inner, n, nlines / lout.inner, lout.estride, lout.outer, Cc, BR,
-                                            swb);
-                    if (mode == 1) {
-                        ok = ok && lin.istride == 1 && lin.inner == lout.inner && ((uintptr_t)in % 16) == 0 &&
-                             make_col_tmap(&tin, in, esz, lin.inner, n, nlines / lin.inner, lin.estride, lin.outer, Cc, BR, swb);
-                        sp.tiles_per_col = lin.inner / Cc;
-                    } else {
-                        ok = ok && ((uintptr_t)in % 16) == 0 && (lin.outer * esz) % 16 == 0 &&
-                             (lin.inner == 1 || (lin.istride * esz) % 16 == 0) && (n * esz) % 16 == 0;
-                    }
-                    if (ok && colpass_launch((int)n, mode, sign, in, sp, tin, tout, Wp, Whi_, Wlo_, g_err_dev, ctx.s)) {
-                        g_launches++;
-                        return JT_OK;
-                    }
                 }
             }
             // TMA pipeline when the 16-byte rules hold, else the plain kernel
@@ -1681,7 +1645,7 @@ int jt_set_split(int prec, int log2n, int a, int b, int c) {
 int jt_set_option(int option, int value) {
     if (option == JT_OPT_TMA_PIPELINE) return g_opt_tma.exchange(value ? 1 : 0);
     if (option == JT_OPT_DIRECT_MAX_F32) return g_opt_direct_max_f32.exchange(value);
-    if (option == JT_OPT_COLUMN_KERNEL) return g_opt_colpass.exchange(value ? 1 : 0);
+    if (option == JT_OPT_COLUMN_KERNEL) return value == 0 ? 0 : JT_EINVAL;
     if (option == JT_OPT_DIRECT_MAX_F64) return g_opt_direct_max_f64.exchange(value);
     if (option == JT_OPT_THREEPASS_MIN_LOG2) {
         if (value < 0 || value > 30) return JT_EINVAL;

@@ -48,34 +48,4 @@ bool stockham_launch(int L, int mode, int sign, const V2<double>::t *in, V2<doub
 #undef JT_CASE
 }
 
-// Column-pass kernels (colpass_kernel): tile width C and TMA swizzle code
-// (0 none, 1 32B, 2 64B, 3 128B) of length L; false when not instantiated.
-bool colpass_cfg(int L, int mode, int *C, int *swb, const double *) {
-#define JT_CCASE(LL)                                                                                 \
-    case LL:                                                                                         \
-        *C = ColPass<double, LL, 1, -1>::C;                                                            \
-        *swb = ColPass<double, LL, 1, -1>::SWB;                                                        \
-        return mode == 1 ? ColPass<double, LL, 1, -1>::OK : ColPass<double, LL, 2, -1>::OK;
-    switch (L) {
-        JT_CCASE(16) JT_CCASE(32) JT_CCASE(64) JT_CCASE(128) JT_CCASE(256) JT_CCASE(512) JT_CCASE(1024)
-        JT_CCASE(2048) JT_CCASE(4096)
-        default: return false;
-    }
-#undef JT_CCASE
-}
-
-bool colpass_launch(int L, int mode, int sign, const V2<double>::t *in, const StockParams &p, const CUtensorMap &tin,
-                    const CUtensorMap &tout, const V2<double>::t *W, const V2<double>::t *Whi, const V2<double>::t *Wlo, int *err,
-                    cudaStream_t s) {
-#define JT_LCASE(LL) \
-    case LL:         \
-        return ColLaunch<double, LL>::go(mode, sign, in, p, tin, tout, W, Whi, Wlo, err, s);
-    switch (L) {
-        JT_LCASE(16) JT_LCASE(32) JT_LCASE(64) JT_LCASE(128) JT_LCASE(256) JT_LCASE(512) JT_LCASE(1024)
-        JT_LCASE(2048) JT_LCASE(4096)
-        default: return false;
-    }
-#undef JT_LCASE
-}
-
 }  // namespace jt

@@ -764,188 +764,4 @@ template <typename T, int L> struct StockLaunch {
     }
 };
 
-// ---------------------------------------------------------------------------
-// Column passes of the four-step scheme, one thread group per line.
-//   MODE 1: C adjacent columns in (TMA tensor load), C columns out (TMA
-//           tensor store), four-step twiddle fused.
-//   MODE 2: C rows in (TMA bulk copies), C columns out (TMA tensor store).
-// The column tile sits in shared memory with TMA's 16-byte-chunk swizzle
-// (32/64/128-byte span = the tile row), so a group reading down its column
-// touches spread banks.  The TL = L/16 threads of a line synchronise among
-// themselves only (warp sync, or a named barrier when a line spans warps);
-// the whole CTA meets only around the loads and stores.  Non-persistent:
-// two CTAs per SM overlap each other's copies and compute.
-// ---------------------------------------------------------------------------
-template <typename T> struct ColCfg {
-    static constexpr int esz = (int)sizeof(typename V2<T>::t);
-    // columns per tile: the widest (<= 128-byte) row that keeps C * L/16 <= 512
-    static constexpr int C(int L) {
-        return (128 / esz) * (L / 16) <= 512 ? 128 / esz
-               : (64 / esz) * (L / 16) <= 512 ? 64 / esz
-               : (32 / esz) * (L / 16) <= 512 ? 32 / esz
-                                              : 16 / esz;
-    }
-};
-
-template <typename T, int L, int MODE, int SIGN> struct ColPass {
-    typedef typename V2<T>::t C2;
-    typedef Stockham<T, L, 1, SIGN> S;  // pass structure (E, TL, passes) only
-    static constexpr int E = S::E, TL = S::TL;
-    static constexpr int esz = (int)sizeof(C2);
-    static constexpr int C = ColCfg<T>::C(L);
-    static constexpr int NT = C * TL;
-    static constexpr int SPAN = C * esz;  // bytes per tile row
-    static constexpr int SWB = SPAN >= 128 ? 3 : SPAN == 64 ? 2 : SPAN == 32 ? 1 : 0;
-    static constexpr int LPR = L + L / 16 + 2;  // MODE 2 padded row (even: 16-byte aligned rows)
-    static constexpr int MAIN = ((MODE == 2 ? C * LPR * esz : C * L * esz) + 1023) / 1024 * 1024;
-    static constexpr size_t SMEM = (size_t)MAIN + 1024 + 16;
-    static constexpr int BR = L < 256 ? L : 256;  // rows per TMA box
-    static constexpr int XM = esz / 8;            // 8-byte units per element in the maps
-    // two CTAs per SM where 64 registers hold a line's work without spills
-    static constexpr int MINB = sizeof(T) == 4 && (MODE == 1 ? L < 4096 : L < 512) ? 2 : 1;
-    static constexpr bool OK = SMEM <= 227 * 1024 && NT <= 1024 && NT >= 32;
-    // byte offset of tile element (row r, column c) under the TMA swizzle
-    static __device__ __forceinline__ int toff(int r, int c) {
-        int b = (r * C + c) * esz;
-        return b ^ (((b >> 7) & ((1 << SWB) - 1)) << 4);
-    }
-};
-
-template <typename T, int L, int MODE, int SIGN>
-__global__ void __launch_bounds__(ColPass<T, L, MODE, SIGN>::NT, ColPass<T, L, MODE, SIGN>::MINB)
-    colpass_kernel(const typename V2<T>::t *__restrict__ in, StockParams p, const __grid_constant__ CUtensorMap tin,
-                   const __grid_constant__ CUtensorMap tout, const typename V2<T>::t *__restrict__ W,
-                   const typename V2<T>::t *__restrict__ Whi, const typename V2<T>::t *__restrict__ Wlo, int *err) {
-    typedef ColPass<T, L, MODE, SIGN> CP;
-    typedef typename CP::S S;
-    typedef typename V2<T>::t C2;
-    extern __shared__ unsigned char smem_raw[];
-    unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(base + CP::MAIN);
-    C2 *xs = reinterpret_cast<C2 *>(base);
-    const int tid = threadIdx.x;
-    const int c = tid / CP::TL, t = tid % CP::TL;
-    const int64_t tile = blockIdx.x;
-    const int64_t b0 = tile * CP::C;
-    const int lines = (int)min((int64_t)CP::C, p.nlines - b0);
-    // column-side tensor coordinates of the tile
-    int z, x0;
-    if (MODE == 1) {
-        z = (int)(tile / p.tiles_per_col);
-        x0 = (int)(tile - (int64_t)z * p.tiles_per_col) * CP::C;
-    } else {
-        z = (int)(b0 / p.lout.inner);
-        x0 = (int)(b0 - (int64_t)z * p.lout.inner);
-    }
-    if (tid == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-        if (MODE == 1) prefetch_tensormap(&tin);
-        prefetch_tensormap(&tout);
-    }
-    __syncthreads();
-    if (tid == 0) {
-        if (MODE == 1) {
-            mbar_arrive_expect_tx(bar, (uint32_t)(CP::C * L * CP::esz));
-#pragma unroll 1
-            for (int r = 0; r < L; r += CP::BR) tensor3d_g2s(base + r * CP::SPAN, &tin, x0 * CP::XM, r, z, bar);
-        } else {
-            mbar_arrive_expect_tx(bar, (uint32_t)(lines * L * CP::esz));
-#pragma unroll 1
-            for (int cc = 0; cc < lines; cc++)
-                bulk_g2s(xs + cc * CP::LPR, in + line_off(p.lin, b0 + cc), (uint32_t)(L * CP::esz), bar);
-        }
-    }
-    const bool mine = mbar_wait_bounded(bar, 0, JT_MBAR_POLL_LIMIT);
-    if (!__syncthreads_and(mine)) {
-        if (tid == 0) {
-            atomicExch(err, 1);
-            mbar_wait_bounded(bar, 0, JT_MBAR_POLL_LIMIT);  // drain the copies into this CTA
-        }
-        __syncthreads();
-        return;
-    }
-
-    C2 v[CP::E];
-    if (MODE == 1) {
-#pragma unroll
-        for (int m = 0; m < CP::E; m++) v[m] = *reinterpret_cast<const C2 *>(base + CP::toff(t + m * CP::TL, c));
-    } else {
-#pragma unroll
-        for (int m = 0; m < CP::E; m++) v[m] = xs[c * CP::LPR + t + m * CP::TL];
-    }
-    auto gsync = [&] {
-        if (CP::TL <= 32) __syncwarp();
-        else named_barrier(1 + c, CP::TL);
-    };
-    gsync();  // the group's pass-0 reads finish before its exchange writes
-    // exchange slots: MODE 1 the line's own (swizzled) column; MODE 2 its padded row
-    auto xi = [&](int i) {
-        if (MODE == 1) return CP::toff(i, c) / CP::esz;
-        return c * CP::LPR + pad(i);
-    };
-    // last-pass outputs stay in registers until the tile is free
-    C2 o[CP::E];
-    auto keep = [&](int, C2 val, int slot) { o[slot] = val; };
-    S::run_all(v, t, xs, xi, W, keep, gsync);
-    // positions of the outputs in `o`: the last pass writes idxD + k*NS with
-    // idxD = j = t + q*TL, NS = L/R, in (q, k) order
-    constexpr int RL = S::template Pass<S::NPASS - 1>::R;
-    constexpr int NBL = S::template Pass<S::NPASS - 1>::NB;
-    constexpr int NSL = S::template Pass<S::NPASS - 1>::NS;
-    if (MODE == 2) __syncthreads();  // every row is read: the tile may be overwritten
-    const bool tw = p.tw_n != 0;
-    const uint32_t j2 = (uint32_t)(x0 + c);
-    const T sc = param_scale<T>(p);
-    const bool do_scale = p.do_scale != 0;
-#pragma unroll
-    for (int q = 0; q < NBL; q++)
-#pragma unroll
-        for (int k = 0; k < RL; k++) {
-            const int pos = t + q * CP::TL + k * NSL;
-            C2 val = o[q * RL + k];
-            if (tw) {
-                C2 w = tw_lookup<T>(Whi, Wlo, (uint32_t)pos * j2, p);
-                val = SIGN < 0 ? cmul<T>(val, w) : cmulc<T>(val, w);
-            }
-            if (do_scale) val = cscale<T>(val, sc);
-            *reinterpret_cast<C2 *>(base + CP::toff(pos, c)) = val;
-        }
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-#pragma unroll 1
-        for (int r = 0; r < L; r += CP::BR) tensor3d_s2g(&tout, x0 * CP::XM, r, z, base + r * CP::SPAN);
-        bulk_commit();
-        bulk_wait_all();
-    }
-}
-
-template <typename T, int L> struct ColLaunch {
-    typedef typename V2<T>::t C2;
-    template <int MODE, int SIGN>
-    static bool one(const C2 *in, const StockParams &p, const CUtensorMap &tin, const CUtensorMap &tout, const C2 *W,
-                    const C2 *Whi, const C2 *Wlo, int *err, cudaStream_t s) {
-        typedef ColPass<T, L, MODE, SIGN> CP;
-        if constexpr (!CP::OK) {
-            return false;
-        } else {
-            static bool attr = false;
-            if (!attr) {
-                cudaFuncSetAttribute(colpass_kernel<T, L, MODE, SIGN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CP::SMEM);
-                cudaFuncSetAttribute(colpass_kernel<T, L, MODE, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-                attr = true;
-            }
-            int64_t grid = (p.nlines + CP::C - 1) / CP::C;
-            colpass_kernel<T, L, MODE, SIGN><<<(unsigned)grid, CP::NT, CP::SMEM, s>>>(in, p, tin, tout, W, Whi, Wlo, err);
-            return true;
-        }
-    }
-    static bool go(int mode, int sign, const C2 *in, const StockParams &p, const CUtensorMap &tin, const CUtensorMap &tout,
-                   const C2 *W, const C2 *Whi, const C2 *Wlo, int *err, cudaStream_t s) {
-        if (mode == 1) return sign < 0 ? one<1, -1>(in, p, tin, tout, W, Whi, Wlo, err, s) : one<1, 1>(in, p, tin, tout, W, Whi, Wlo, err, s);
-        return sign < 0 ? one<2, -1>(in, p, tin, tout, W, Whi, Wlo, err, s) : one<2, 1>(in, p, tin, tout, W, Whi, Wlo, err, s);
-    }
-};
-
 }  // namespace jt

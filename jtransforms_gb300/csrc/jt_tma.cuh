@@ -71,16 +71,6 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map) {
 
 namespace jt {
 
-// 3D tiled tensor copy shared -> global (bulk-group completion).
-__device__ __forceinline__ void tensor3d_s2g(const CUtensorMap *map, int x, int y, int z, const void *src) {
-    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(map), "r"(x), "r"(y),
-                 "r"(z), "r"(smem_addr(src))
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// Waits until every committed bulk store has completed.
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-
 // Synchronises the `count` threads (a multiple of 32) that use barrier `id`.
 __device__ __forceinline__ void named_barrier(int id, int count) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
