@@ -19,6 +19,7 @@ workload, on a bounded sample of each batch.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -313,6 +314,26 @@ def other_workloads(args, peak, flush, stream):
     out = {}
     rng = np.random.default_rng(SEED)
     steps, warm = max(args.steps, 3), args.warmup
+    # compute rooflines: CUDA-core FMA throughput measured on this GPU
+    fma = {}
+    for key, prec in (("fp64", N.FLOAT64), ("fp32", N.FLOAT32)):
+        v = ctypes.c_double()
+        if N.load().jt_fma_peak(prec, ctypes.byref(v)) == N.OK:
+            fma[key] = v.value
+    out["fma_peak_GFLOPs"] = fma
+
+    def bound(entry, flops, bytes_alg, ms, prec):
+        # the roofline of a Double (or Float) workload: min(HBM x intensity,
+        # CUDA-core FMA peak) on the convention's flop count
+        cpeak = fma.get(prec)
+        gf = flops / (ms * 1e-3) / 1e9
+        hbm_lim = peak * flops / bytes_alg
+        entry["hbm_frac"] = (bytes_alg / (ms * 1e-3) / 1e9) / peak
+        if cpeak:
+            entry[f"{prec}_frac_nominal"] = gf / cpeak
+            entry["attainable_GFLOP/s"] = min(hbm_lim, cpeak)
+            entry["binding"] = prec if cpeak < hbm_lim else "hbm"
+            entry["frac_of_attainable"] = gf / min(hbm_lim, cpeak)
 
     def measure(name, plan, op, buf, batch, dist, scale, flops, bytes_alg, unit_note, extra_fn=None):
         pristine = buf.clone()
@@ -322,7 +343,8 @@ def other_workloads(args, peak, flush, stream):
         t = timed_calls(fns, lambda i: buf.copy_(pristine), flush, steps, warm, stream)[0]
         ms = statistics.median(t)
         out[name] = {"value": flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms": ms, "best_ms": min(t),
-                     "hbm_frac": (bytes_alg / (ms * 1e-3) / 1e9) / peak, "flops": unit_note}
+                     "flops": unit_note}
+        bound(out[name], flops, bytes_alg, ms, "fp64" if buf.dtype == torch.float64 else "fp32")
 
     # config 1: 256 x DoubleFFT_1D(4096) complexForward then complexInverse(scale=true)
     n, B = 4096, 256
@@ -337,7 +359,8 @@ def other_workloads(args, peak, flush, stream):
     ms = statistics.median(t)
     out["c1_DoubleFFT_1D_4096x256_fwd_inv"] = {
         "value": 2 * flops_c2c(n, B) / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms": ms,
-        "hbm_frac": (4 * 16 * n * B / (ms * 1e-3) / 1e9) / peak, "flops": "5N log2N x2 directions"}
+        "flops": "5N log2N x2 directions"}
+    bound(out["c1_DoubleFFT_1D_4096x256_fwd_inv"], 2 * flops_c2c(n, B), 4 * 16 * n * B, ms, "fp64")
 
     # config 2a: FloatFFT_2D(2048, 2048).realForward on a blob image
     img = blob_image(2048, rng).astype(np.float32).ravel()
@@ -517,21 +540,44 @@ def run_ours(args, world, rank, local):
                                            "algorithm": ["direct", "two-pass", "bluestein", "trivial", "three-pass"][plans[i].plan.algorithm(0)]}
                 for i, (n, ms) in enumerate(zip(SIZES, per_size_ms))}
 
-    # error against FP64 of one transform per size: input set (a) = the timed
-    # data, set (b) = 60 dB dynamic range
-    def rel_err(plan, xin):
-        x = xin.double()
+    # the output of the last timed call of each size, checked against FP64:
+    # the first, middle and last transform of the batch and one drawn at random
+    def errs(got_f32, xin_f32):
+        x = xin_f32.double()
         ref = torch.fft.fft(torch.complex(x[0::2], x[1::2]))
+        got = torch.complex(got_f32[0::2].double(), got_f32[1::2].double())
+        d = got - ref
+        return (float(torch.linalg.norm(d) / torch.linalg.norm(ref)),
+                float(d.abs().max() / ref.abs().max()))
+
+    timed_check = {}
+    pick = np.random.default_rng(SEED + 7)
+    for i, n in enumerate(SIZES):
+        b = ELEMS // n
+        worst = [0.0, 0.0]
+        ts = sorted({0, b // 2, b - 1, int(pick.integers(0, b))})
+        for t in ts:
+            e = errs(work[i][2 * n * t: 2 * n * (t + 1)], pristine[i][2 * n * t: 2 * n * (t + 1)])
+            worst = [max(worst[0], e[0]), max(worst[1], e[1])]
+        timed_check[f"2^{int(math.log2(n))}"] = {"transforms_checked": ts,
+                                                 "max_rel_l2_vs_fp64": worst[0], "max_rel_max_err_vs_fp64": worst[1],
+                                                 "tol_4eps_log2n": 4 * 2.0 ** -23 * math.log2(n)}
+
+    # error against FP64 of one transform per size: input set (a) = the timed
+    # data, set (b) = 60 dB dynamic range; relative L2 and max error
+    # (max |got - ref| / max |ref|)
+    def rel_err(plan, xin, both=False):
         w = xin.clone()
         plan.execute(N.COMPLEX_FORWARD, w, 0, False)
-        got = torch.complex(w[0::2].double(), w[1::2].double())
-        return float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        e = errs(w, xin)
+        return e if both else e[0]
 
-    err, err_b, set_b = {}, {}, []
+    err, err_b, set_b, err_max, err_b_max = {}, {}, [], {}, {}
     for i, n in enumerate(SIZES):
         set_b.append(sixty_db(n, g))
-        err[f"2^{int(math.log2(n))}"] = rel_err(plans[i].plan, pristine[i][: 2 * n])
-        err_b[f"2^{int(math.log2(n))}"] = rel_err(plans[i].plan, set_b[i])
+        key = f"2^{int(math.log2(n))}"
+        err[key], err_max[key] = rel_err(plans[i].plan, pristine[i][: 2 * n], True)
+        err_b[key], err_b_max[key] = rel_err(plans[i].plan, set_b[i], True)
 
     # split-operand tensor-core mode beside plain FP32 (row lengths 16..2048)
     tc = {}
@@ -588,6 +634,8 @@ def run_ours(args, world, rank, local):
                          "algorithmic_bytes_per_call": 2 * 8 * ELEMS,
                          "algorithmic_bytes_per_step": bytes_step},
             "per_size": per_size, "rel_l2_vs_fp64": err, "rel_l2_vs_fp64_set_b": err_b,
+            "rel_max_err_vs_fp64": err_max, "rel_max_err_vs_fp64_set_b": err_b_max,
+            "timed_output_check": timed_check,
             "tc_split": {"per_size": tc,
                          "scheme": "radix-16 stages as M128 N32 tcgen05 kind::tf32 products, TF32 head + FP32 remainder, "
                                    "3 products hi*hi + lo*hi + hi*lo, FP32 accumulate in tensor memory; twiddles and "

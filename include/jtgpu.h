@@ -119,16 +119,27 @@ int jt_execute_device(jt_plan *plan, int op, void *dev_array, int64_t batch,
  * for callers that cannot allocate device memory when they transform, such as
  * code inside CUDA stream capture (cudaMalloc is not allowed there) or with a
  * fixed memory budget.  Scratch comes from one fixed 32 MiB device array per
- * GPU: two-pass lengths need n*8 (float) / n*16 (double) bytes of it, so
- * n <= 2^22 / 2^21 there; Bluestein lengths are refused with JT_ESCRATCH.
- * Calls share the array, so calls that overlap on the GPU race.  The first
- * call on a device looks up the array's address: make it before any stream
- * capture.  Asynchronous on `stream` (NULL = the default stream). */
+ * GPU: two- and three-pass lengths need n*8 (float) / n*16 (double) bytes of
+ * it, so n <= 2^22 / 2^21 there; Bluestein lengths are refused with
+ * JT_ESCRATCH.  Calls share the array, so calls that overlap on the GPU race.
+ * The first call on a device looks up the array's address: make it before any
+ * stream capture.  The plan must be used on the device it was created on
+ * (JT_EINVAL otherwise).  Asynchronous on `stream` (NULL = the default
+ * stream); a timed-out device wait is reported by jt_check_error after the
+ * caller's own synchronisation. */
 int jt_execute_device_noalloc(jt_plan *plan, int op, const void *dev_in, void *dev_out, int64_t batch, int scale,
                               void *stream);
 
 /* Waits for the calling thread's stream; returns JT_ECUDA on a device error. */
 int jt_synchronize(void);
+
+/* Reads and clears the device error flag that a kernel raises when one of
+ * its bounded waits gives up: JT_ETIMEOUT if it was raised, else JT_OK.
+ * For callers that synchronise their own streams or graphs (after
+ * jt_execute_device or jt_execute_device_noalloc); jt_synchronize and the
+ * host-array calls check it themselves.  No counterpart in the reference
+ * (worker failures are logged there, fft/DoubleFFT_1D.java:711-715). */
+int jt_check_error(void);
 
 /* Mixed-size batch (work descriptors of several plans) -------------------- */
 typedef struct jt_batch jt_batch;
@@ -162,6 +173,15 @@ int jt_batch_destroy(jt_batch *batch);
                                        near-equal lengths (default 21; 0: only beyond 2^24, where
                                        every power of two up to 2^32 takes three).  Read when a
                                        plan is created. */
+#define JT_OPT_ARENA_LIMIT_MB 7   /* device scratch budget per call in MiB (default 0: no limit): a call
+                                     whose scratch (host-array ring buffers included) needs more
+                                     returns JT_ENOMEM before it launches anything */
+#define JT_OPT_BATCH_WAIT_POLLS 8 /* polls (64 ns apart) of a batch kernel's dependency wait before it gives
+                                     up with JT_ETIMEOUT (default 2^24, about a second); read by
+                                     jt_batch_create */
+#define JT_OPT_BATCH_STALL_TEST 9 /* failure-path test hook (default 0): 1 makes jt_batch_create add a step
+                                     that never runs as the dependency of every transform's first step,
+                                     so the waits run out and the run reports JT_ETIMEOUT */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 
@@ -180,6 +200,10 @@ int64_t jt_launch_count(int reset);
 /* Algorithm the plan uses along axis `axis` for length-n complex work:
  * 0 direct in-CTA, 1 two-pass, 2 Bluestein, 3 trivial, 4 three-pass. */
 int jt_plan_algorithm(const jt_plan *plan, int axis);
+/* Measured CUDA-core FMA throughput of the current GPU in GFLOP/s (one FMA =
+ * two flops) for `prec`: the compute roofline of the Double (FP64) and Float
+ * paths.  No counterpart in the reference. */
+int jt_fma_peak(int prec, double *gflops);
 
 #ifdef __cplusplus
 }

@@ -13,5 +13,6 @@ from .r2r import (DoubleDCT_1D, DoubleDCT_2D, DoubleDCT_3D, DoubleDHT_1D,  # noq
                   DoubleDST_3D, FloatDCT_1D, FloatDCT_2D, FloatDCT_3D,
                   FloatDHT_1D, FloatDHT_2D, FloatDHT_3D, FloatDST_1D,
                   FloatDST_2D, FloatDST_3D)
+from .real_fft_utils import RealFFTUtils_2D, RealFFTUtils_3D  # noqa: F401
 from . import utils  # noqa: F401
 from .utils import CommonUtils, ConcurrencyUtils  # noqa: F401

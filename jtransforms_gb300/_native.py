@@ -38,6 +38,7 @@ SIGNATURES = {
     "jt_execute_batch": (_I, [_P, _I, _P, _L, _L, _L, _L, _I]),
     "jt_execute_device": (_I, [_P, _I, _P, _L, _L, _I, _P]),
     "jt_synchronize": (_I, []),
+    "jt_check_error": (_I, []),
     "jt_batch_create": (_I, [_I, ctypes.POINTER(_P), ctypes.POINTER(_I), ctypes.POINTER(_P), ctypes.POINTER(_I), ctypes.POINTER(_P)]),
     "jt_batch_run": (_I, [_P, _P]),
     "jt_batch_run_per_transform": (_I, [_P, _P]),
@@ -49,9 +50,11 @@ SIGNATURES = {
     "jt_plan_algorithm": (_I, [_P, _I]),
     "jt_set_option": (_I, [_I, _I]),
     "jt_execute_device_noalloc": (_I, [_P, _I, _P, _P, _L, _I, _P]),
+    "jt_fma_peak": (_I, [_I, ctypes.POINTER(ctypes.c_double)]),
 }
 OPT_TMA_PIPELINE, OPT_DIRECT_MAX_F32, OPT_DIRECT_MAX_F64, OPT_COLUMN_KERNEL, OPT_TWOPASS_CHUNK_MB = 0, 1, 2, 3, 4
 OPT_THREEPASS_MIN_LOG2, OPT_HOST_PIECE_MB = 5, 6
+OPT_ARENA_LIMIT_MB, OPT_BATCH_WAIT_POLLS, OPT_BATCH_STALL_TEST = 7, 8, 9
 
 _lib = None
 _lock = threading.Lock()

@@ -144,10 +144,11 @@ __device__ __forceinline__ int ld_acquire_gpu(const int *p) {
     return v;
 }
 
-#define JT_BATCH_WAIT_LIMIT (1 << 24)
-
+// wait_polls: polls of a dependency wait (64 ns apart) before it gives up;
+// the library's default, 2^24, is about a second
 __global__ void __launch_bounds__(JT_BATCH_THREADS, 1)
-    batch_kernel(const BOp *__restrict__ ops, const BTask *__restrict__ tasks, int ntasks, int *head, int *done, int *err) {
+    batch_kernel(const BOp *__restrict__ ops, const BTask *__restrict__ tasks, int ntasks, int *head, int *done, int *err,
+                 int wait_polls) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_task;
     __shared__ int s_ok;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(JT_BATCH_THREADS, 1)
                 const int need = ops[o.dep].ntasks;
                 int it = 0;
                 while (ld_acquire_gpu(&done[o.dep]) < need) {
-                    if (++it > JT_BATCH_WAIT_LIMIT) {
+                    if (++it > wait_polls) {
                         ok = 0;
                         atomicExch(err, 1);
                         break;

@@ -143,6 +143,21 @@ static bool g_split_override_init = [] {
 }();
 static std::once_flag g_dev_once;
 static int g_dev_status = JT_OK;
+// Plan tables are built on one non-blocking setup stream, and a plan is
+// ready once that stream has finished (a wait on the setup stream only:
+// work on other streams is neither waited for nor stalled).
+static cudaStream_t g_setup = nullptr;
+static std::atomic<uint64_t> g_setup_seq{0};  // table builds so far
+// bumped when an option that changes plan choice changes: cached tables of
+// an older generation are not reused
+static std::atomic<uint64_t> g_plan_gen{0};
+// largest per-thread scratch arena in bytes (0: no limit)
+static std::atomic<int64_t> g_opt_arena_limit{0};
+// polls of a batch dependency wait before it gives up, and a test hook that
+// makes the first step of every batch transform wait on a step that is never
+// queued (a flag nothing sets), so the waits run out
+static std::atomic<int> g_opt_batch_wait{1 << 24};
+static std::atomic<int> g_opt_batch_inject{0};
 
 static int device_init() {
     std::call_once(g_dev_once, [] {
@@ -155,7 +170,8 @@ static int device_init() {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (cudaMalloc(&g_err_dev, sizeof(int)) != cudaSuccess || cudaMemset(g_err_dev, 0, sizeof(int)) != cudaSuccess) {
+        if (cudaMalloc(&g_err_dev, sizeof(int)) != cudaSuccess || cudaMemset(g_err_dev, 0, sizeof(int)) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&g_setup, cudaStreamNonBlocking) != cudaSuccess) {
             g_dev_status = JT_ECUDA;
             return;
         }
@@ -287,7 +303,7 @@ template <typename T> struct Fft1 {
 
     static int make_roots(C2 **out, int64_t count, int64_t num, int64_t den) {
         JT_CU(cudaMalloc(out, sizeof(C2) * std::max<int64_t>(count, 1)));
-        roots_kernel<T><<<(unsigned)cdiv(count, 256), 256>>>(*out, count, num, den);
+        roots_kernel<T><<<(unsigned)cdiv(count, 256), 256, 0, g_setup>>>(*out, count, num, den);
         g_launches++;
         JT_CU(cudaGetLastError());
         return JT_OK;
@@ -297,7 +313,7 @@ template <typename T> struct Fft1 {
         const int count = stock_tw_count(L);
         JT_CU(cudaMalloc(out, sizeof(C2) * std::max(count, 1)));
         if (count > 0) {
-            passtw_kernel<T><<<(unsigned)cdiv(count, 256), 256>>>(*out, L);
+            passtw_kernel<T><<<(unsigned)cdiv(count, 256), 256, 0, g_setup>>>(*out, L);
             g_launches++;
             JT_CU(cudaGetLastError());
         }
@@ -694,8 +710,8 @@ template <typename T> int Fft1<T>::make_chirp() {
     JT_CU(cudaMalloc(&bk1, sizeof(C2) * n));
     JT_CU(cudaMalloc(&bk2, sizeof(C2) * nB));
     double2 *b64 = nullptr;
-    JT_CU(cudaMalloc(&b64, sizeof(double2) * nB));
-    chirp_kernel<T><<<(unsigned)cdiv(nB, 256), 256>>>(bk1, b64, n, nB);
+    JT_CU(cudaMallocAsync(&b64, sizeof(double2) * nB, g_setup));
+    chirp_kernel<T><<<(unsigned)cdiv(nB, 256), 256, 0, g_setup>>>(bk1, b64, n, nB);
     g_launches++;
     int st = JT_OK;
     {
@@ -704,31 +720,87 @@ template <typename T> int Fft1<T>::make_chirp() {
         if (st == JT_OK) {
             Arena ar;
             Ctx c;
-            c.s = nullptr;
+            c.s = g_setup;
             c.ws = &ar;
             c.dry = true;
             st = f64->exec(c, b64, nB, b64, nB, 1, -1, 1.0);
             if (st == JT_OK) {
                 if (ar.peak) {
-                    if (cudaMalloc(&ar.base, ar.peak) != cudaSuccess) st = JT_ENOMEM;
+                    if (cudaMallocAsync((void **)&ar.base, ar.peak, g_setup) != cudaSuccess) st = JT_ENOMEM;
                     ar.cap = ar.peak;
                 }
                 ar.used = 0;
                 c.dry = false;
                 if (st == JT_OK) st = f64->exec(c, b64, nB, b64, nB, 1, -1, 1.0);
-                cudaDeviceSynchronize();
-                if (ar.base) cudaFree(ar.base);
+                if (ar.base) cudaFreeAsync(ar.base, g_setup);
             }
+            // the FP64 plan's own tables are freed when it goes out of scope:
+            // its kernels on the setup stream finish first
+            cudaStreamSynchronize(g_setup);
         }
     }
     if (st == JT_OK) {
-        d2t_kernel<T><<<(unsigned)cdiv(nB, 256), 256>>>(bk2, b64, nB);
+        d2t_kernel<T><<<(unsigned)cdiv(nB, 256), 256, 0, g_setup>>>(bk2, b64, nB);
         g_launches++;
     }
-    cudaDeviceSynchronize();
-    cudaFree(b64);
+    cudaFreeAsync(b64, g_setup);
     JT_CU(cudaGetLastError());
     return st;
+}
+
+// ---------------------------------------------------------------------------
+// Table cache.  The per-length objects below (complex, real, DCT/DST and DHT
+// lines) and their device tables are shared by every jt_plan that needs
+// them, keyed by (length, planning generation): a second DoubleFFT_1D(4096)
+// builds nothing.  Entries that no plan holds any more are kept, least
+// recently used first out, up to kCacheIdleMax per object type.
+// ---------------------------------------------------------------------------
+static std::recursive_mutex g_cache_mu;
+static const int kCacheIdleMax = 32;
+
+template <typename X> struct TableCache {
+    struct Entry {
+        std::shared_ptr<X> obj;
+        uint64_t tick;
+    };
+    std::map<std::pair<int64_t, uint64_t>, Entry> m;
+    uint64_t tick = 0;
+    static TableCache &get() {
+        static TableCache c;
+        return c;
+    }
+};
+
+template <typename X> static int cached(int64_t n, std::shared_ptr<X> &out) {
+    std::lock_guard<std::recursive_mutex> g(g_cache_mu);
+    TableCache<X> &c = TableCache<X>::get();
+    const auto key = std::make_pair(n, g_plan_gen.load());
+    auto it = c.m.find(key);
+    if (it != c.m.end()) {
+        it->second.tick = ++c.tick;
+        out = it->second.obj;
+        return JT_OK;
+    }
+    std::unique_ptr<X> u;
+    JT_TRY(X::create(n, u));
+    g_setup_seq++;
+    std::shared_ptr<X> sp(u.release());
+    c.m.emplace(key, typename TableCache<X>::Entry{sp, ++c.tick});
+    out = sp;
+    for (;;) {
+        int idle = 0;
+        auto victim = c.m.end();
+        for (auto e = c.m.begin(); e != c.m.end(); ++e)
+            if (e->second.obj.use_count() == 1) {
+                idle++;
+                if (victim == c.m.end() || e->second.tick < victim->second.tick) victim = e;
+            }
+        if (idle <= kCacheIdleMax) break;
+        // kernels of a destroyed plan may still read the victim's tables
+        JT_CU(cudaDeviceSynchronize());
+        c.m.erase(victim);
+    }
+    return JT_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -737,7 +809,7 @@ template <typename T> int Fft1<T>::make_chirp() {
 template <typename T> struct Real1 {
     typedef typename V2<T>::t C2;
     int64_t n = 0;
-    std::unique_ptr<Fft1<T>> half, full;
+    std::shared_ptr<Fft1<T>> half, full;
     C2 *Wr = nullptr;
     ~Real1() {
         if (Wr) cudaFree(Wr);
@@ -747,10 +819,10 @@ template <typename T> struct Real1 {
         if (!r) return JT_ENOMEM;
         r->n = n;
         if (n >= 2 && n % 2 == 0) {
-            JT_TRY(Fft1<T>::create(n / 2, r->half));
+            JT_TRY(cached<Fft1<T>>(n / 2, r->half));
             JT_TRY(Fft1<T>::make_roots(&r->Wr, n / 4 + 1, 1, n));
         } else if (n > 1) {
-            JT_TRY(Fft1<T>::create(n, r->full));
+            JT_TRY(cached<Fft1<T>>(n, r->full));
         }
         out = std::move(r);
         return JT_OK;
@@ -877,7 +949,7 @@ template <typename T> struct Real1 {
 template <typename T> struct Dct1 {
     typedef typename V2<T>::t C2;
     int64_t n = 0;
-    std::unique_ptr<Real1<T>> rf;
+    std::shared_ptr<Real1<T>> rf;
     C2 *Wd = nullptr;
     ~Dct1() {
         if (Wd) cudaFree(Wd);
@@ -887,7 +959,7 @@ template <typename T> struct Dct1 {
         if (!d) return JT_ENOMEM;
         d->n = n;
         if (n > 1) {
-            JT_TRY(Real1<T>::create(n, d->rf));
+            JT_TRY(cached<Real1<T>>(n, d->rf));
             JT_TRY(Fft1<T>::make_roots(&d->Wd, n, 1, 4 * n));  // e^{-i pi k/(2n)}
         }
         out = std::move(d);
@@ -955,12 +1027,12 @@ template <typename T> struct Dct1 {
 // DHT (dht/DoubleDHT_1D.java:94-159, :255-276)
 template <typename T> struct Dht1 {
     int64_t n = 0;
-    std::unique_ptr<Real1<T>> rf;
+    std::shared_ptr<Real1<T>> rf;
     static int create(int64_t n, std::unique_ptr<Dht1> &out) {
         std::unique_ptr<Dht1> d(new (std::nothrow) Dht1());
         if (!d) return JT_ENOMEM;
         d->n = n;
-        if (n > 1) JT_TRY(Real1<T>::create(n, d->rf));
+        if (n > 1) JT_TRY(cached<Real1<T>>(n, d->rf));
         out = std::move(d);
         return JT_OK;
     }
@@ -992,55 +1064,38 @@ template <typename T> struct PlanImpl {
     int64_t dims[3] = {1, 1, 1};
     int64_t N = 1;
     std::mutex mu;
-    // lazily built per axis length
-    std::map<int64_t, std::unique_ptr<Fft1<T>>> fft;
-    std::map<int64_t, std::unique_ptr<Real1<T>>> real;
-    std::map<int64_t, std::unique_ptr<Dct1<T>>> dct;
-    std::map<int64_t, std::unique_ptr<Dht1<T>>> dht;
+    // per axis length, from the table cache (shared with other plans)
+    std::map<int64_t, std::shared_ptr<Fft1<T>>> fft;
+    std::map<int64_t, std::shared_ptr<Real1<T>>> real;
+    std::map<int64_t, std::shared_ptr<Dct1<T>>> dct;
+    std::map<int64_t, std::shared_ptr<Dht1<T>>> dht;
+    template <typename X> static int get(std::map<int64_t, std::shared_ptr<X>> &m, int64_t n, X **out) {
+        auto it = m.find(n);
+        if (it == m.end()) {
+            std::shared_ptr<X> f;
+            JT_TRY(cached<X>(n, f));
+            it = m.emplace(n, std::move(f)).first;
+        }
+        *out = it->second.get();
+        return JT_OK;
+    }
+    int get_fft(int64_t n, Fft1<T> **out) { return get(fft, n, out); }
+    int get_real(int64_t n, Real1<T> **out) { return get(real, n, out); }
+    int get_dct(int64_t n, Dct1<T> **out) { return get(dct, n, out); }
+    int get_dht(int64_t n, Dht1<T> **out) { return get(dht, n, out); }
 
-    int get_fft(int64_t n, Fft1<T> **out) {
-        auto it = fft.find(n);
-        if (it == fft.end()) {
-            std::unique_ptr<Fft1<T>> f;
-            JT_TRY(Fft1<T>::create(n, f));
-            it = fft.emplace(n, std::move(f)).first;
-        }
-        *out = it->second.get();
-        return JT_OK;
-    }
-    int get_real(int64_t n, Real1<T> **out) {
-        auto it = real.find(n);
-        if (it == real.end()) {
-            std::unique_ptr<Real1<T>> f;
-            JT_TRY(Real1<T>::create(n, f));
-            it = real.emplace(n, std::move(f)).first;
-        }
-        *out = it->second.get();
-        return JT_OK;
-    }
-    int get_dct(int64_t n, Dct1<T> **out) {
-        auto it = dct.find(n);
-        if (it == dct.end()) {
-            std::unique_ptr<Dct1<T>> f;
-            JT_TRY(Dct1<T>::create(n, f));
-            it = dct.emplace(n, std::move(f)).first;
-        }
-        *out = it->second.get();
-        return JT_OK;
-    }
-    int get_dht(int64_t n, Dht1<T> **out) {
-        auto it = dht.find(n);
-        if (it == dht.end()) {
-            std::unique_ptr<Dht1<T>> f;
-            JT_TRY(Dht1<T>::create(n, f));
-            it = dht.emplace(n, std::move(f)).first;
-        }
-        *out = it->second.get();
-        return JT_OK;
-    }
-
-    // Builds every table `op` needs (called under the mutex, outside streams).
+    // Builds (or takes from the cache) every table `op` needs, under the
+    // mutex; when anything was built, waits for the setup stream.
     int prepare(int op) {
+        const uint64_t seq0 = g_setup_seq.load();
+        int st = prepare_locked(op);
+        if (st == JT_OK && g_setup_seq.load() != seq0) {
+            JT_CU(cudaStreamSynchronize(g_setup));
+            JT_CU(cudaGetLastError());
+        }
+        return st;
+    }
+    int prepare_locked(int op) {
         std::lock_guard<std::mutex> g(mu);
         Fft1<T> *f;
         Real1<T> *r;
@@ -1269,6 +1324,7 @@ struct jt_plan {
     int kind, prec, nd;
     int64_t dims[3];
     int mode;
+    int device;  // the device current at jt_plan_create: its tables live there
     void *impl;
 };
 
@@ -1314,6 +1370,12 @@ int ensure_copy_streams() {
 
 int ensure_arena(size_t bytes) {
     Arena &a = t_state.arena;
+    // a call needing more scratch than the limit fails, whatever the arena holds
+    const int64_t lim = g_opt_arena_limit.load();
+    if (lim > 0 && (int64_t)bytes > lim) {
+        g_last_cuda = (int)cudaErrorMemoryAllocation;
+        return JT_ENOMEM;
+    }
     if (bytes <= a.cap) return JT_OK;
     if (a.base) {
         cudaStreamSynchronize(t_state.stream);
@@ -1490,6 +1552,8 @@ int jt_plan_create(int kind, int prec, int ndim, const int64_t *dims, jt_plan **
     p->prec = prec;
     p->nd = ndim;
     p->mode = JT_MODE_FP32;
+    p->device = 0;
+    cudaGetDevice(&p->device);
     int64_t N = 1;
     for (int d = 0; d < 3; d++) p->dims[d] = d < ndim ? dims[d] : 1;
     for (int d = 0; d < ndim; d++) N *= dims[d];
@@ -1516,7 +1580,6 @@ int jt_plan_create(int kind, int prec, int ndim, const int64_t *dims, jt_plan **
     int main_op = kind == JT_FFT ? JT_COMPLEX_FORWARD : JT_FORWARD;
     if (prec == JT_FLOAT32) st = impl_of<float>(p)->prepare(main_op);
     else st = impl_of<double>(p)->prepare(main_op);
-    if (st == JT_OK && cudaDeviceSynchronize() != cudaSuccess) st = JT_ECUDA;
     if (st != JT_OK) {
         jt_plan_destroy(p);
         return st;
@@ -1527,7 +1590,8 @@ int jt_plan_create(int kind, int prec, int ndim, const int64_t *dims, jt_plan **
 
 int jt_plan_destroy(jt_plan *p) {
     if (!p) return JT_EINVAL;
-    cudaDeviceSynchronize();
+    // the plan's tables stay in the table cache: nothing is freed here, so
+    // kernels still running with them are unaffected and nothing waits
     if (p->prec == JT_FLOAT32) delete (PlanImpl<float> *)p->impl;
     else delete (PlanImpl<double> *)p->impl;
     delete p;
@@ -1606,6 +1670,11 @@ int jt_synchronize(void) {
     return check_err_flag();
 }
 
+int jt_check_error(void) {
+    JT_TRY(device_init());
+    return check_err_flag();
+}
+
 const char *jt_strerror(int s) {
     switch (s) {
         case JT_OK: return "ok";
@@ -1629,6 +1698,7 @@ int jt_set_split(int prec, int log2n, int a, int b, int c) {
     if ((prec != JT_FLOAT32 && prec != JT_FLOAT64) || log2n < 4 || log2n > JT_SPLIT_MAX_LOG2) return JT_EINVAL;
     signed char *e = g_split_override[prec == JT_FLOAT32 ? 0 : 1][log2n];
     if (a < 0) {
+        if (e[0] >= 0) g_plan_gen++;
         e[0] = e[1] = e[2] = -1;
         return JT_OK;
     }
@@ -1639,17 +1709,32 @@ int jt_set_split(int prec, int log2n, int a, int b, int c) {
     e[0] = (signed char)a;
     e[1] = (signed char)b;
     e[2] = (signed char)c;
+    g_plan_gen++;
     return JT_OK;
 }
 
 int jt_set_option(int option, int value) {
     if (option == JT_OPT_TMA_PIPELINE) return g_opt_tma.exchange(value ? 1 : 0);
-    if (option == JT_OPT_DIRECT_MAX_F32) return g_opt_direct_max_f32.exchange(value);
+    if (option == JT_OPT_DIRECT_MAX_F32 || option == JT_OPT_DIRECT_MAX_F64) {
+        const int prev = (option == JT_OPT_DIRECT_MAX_F32 ? g_opt_direct_max_f32 : g_opt_direct_max_f64).exchange(value);
+        if (prev != value) g_plan_gen++;  // plans created from now on choose again
+        return prev;
+    }
     if (option == JT_OPT_COLUMN_KERNEL) return value == 0 ? 0 : JT_EINVAL;
-    if (option == JT_OPT_DIRECT_MAX_F64) return g_opt_direct_max_f64.exchange(value);
+    if (option == JT_OPT_ARENA_LIMIT_MB) {
+        if (value < 0) return JT_EINVAL;
+        return (int)(g_opt_arena_limit.exchange((int64_t)value << 20) >> 20);
+    }
+    if (option == JT_OPT_BATCH_WAIT_POLLS) {
+        if (value < 1) return JT_EINVAL;
+        return g_opt_batch_wait.exchange(value);
+    }
+    if (option == JT_OPT_BATCH_STALL_TEST) return g_opt_batch_inject.exchange(value ? 1 : 0);
     if (option == JT_OPT_THREEPASS_MIN_LOG2) {
         if (value < 0 || value > 30) return JT_EINVAL;
-        const int64_t prev = g_opt_threepass_min.exchange(value ? (int64_t)1 << value : 0);
+        const int64_t nv = value ? (int64_t)1 << value : 0;
+        const int64_t prev = g_opt_threepass_min.exchange(nv);
+        if (prev != nv) g_plan_gen++;
         int lg = 0;
         while (prev && ((int64_t)1 << lg) < prev) lg++;
         return prev ? lg : 0;
@@ -1691,6 +1776,7 @@ struct jt_batch {
     char *scratch_d = nullptr;  // double transforms' scratch
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
+    int wait_polls = 1 << 24;  // polls of a dependency wait before it gives up
     ~jt_batch() {
         if (graph) cudaGraphExecDestroy(graph);
         for (void *p : {(void *)d_ops, (void *)d_tasks, (void *)d_done, (void *)d_head, (void *)scratch, (void *)scratch_d})
@@ -1775,6 +1861,18 @@ int jt_batch_create(int count, jt_plan *const *plans, const int *ops, void *cons
     std::vector<std::vector<int>> chains(count);
     JT_TRY(batch_record<float>(b.get(), rec, chains));
     JT_TRY(batch_record<double>(b.get(), rec, chains));
+    b->wait_polls = g_opt_batch_wait.load();
+    if (g_opt_batch_inject.load() && !rec.empty()) {
+        // failure-path test: a step no task ever runs, made the dependency
+        // of every transform's first step, so their waits run out
+        BOp never = elem_op<float>(EK_SCALE, 0, 0);
+        never.ntasks = 1;
+        never.dep = -1;
+        rec.push_back(never);
+        const int phantom = (int)rec.size() - 1;
+        for (auto &c : chains)
+            if (!c.empty()) rec[c[0]].dep = phantom;
+    }
     // tasks, stage by stage: every transform's first step, then the second...
     std::vector<BTask> tasks;
     size_t maxlen = 0;
@@ -1816,7 +1914,7 @@ int jt_batch_run(jt_batch *b, void *stream) {
     JT_CU(cudaMemsetAsync(b->d_done, 0, sizeof(int) * b->nops, s));
     JT_CU(cudaMemsetAsync(b->d_head, 0, sizeof(int), s));
     batch_kernel<<<b->grid, JT_BATCH_THREADS, std::max(b->smem, 1), s>>>(b->d_ops, b->d_tasks, b->ntasks, b->d_head, b->d_done,
-                                                                          g_err_dev);
+                                                                          g_err_dev, b->wait_polls);
     g_launches++;
     JT_CU(cudaGetLastError());
     return JT_OK;
@@ -1891,11 +1989,19 @@ int jt_batch_destroy(jt_batch *b) {
 // Each GPU that loads the library holds that array until the process exits.
 //
 // Limit: the scratch is JT_NOALLOC_SCRATCH_BYTES (32 MiB).  Lengths that
-// need the two-pass scheme need one length's worth of complex scratch per
-// transform in flight: n * 8 bytes (float) or n * 16 bytes (double) must fit,
-// so n <= 2^22 (float) / 2^21 (double) there.  Lengths done in one pass need
-// none.  Bluestein lengths are rejected: their scratch would not be bounded
-// by one transform.
+// need the two- or three-pass scheme need one length's worth of complex
+// scratch per transform in flight: n * 8 bytes (float) or n * 16 bytes
+// (double) must fit, so n <= 2^22 (float) / 2^21 (double) there.  Lengths
+// done in one pass need none.  Bluestein lengths are rejected: their scratch
+// would not be bounded by one transform.
+//
+// The plan must be used on the device that was current when it was created
+// (its tables live there); another current device gives JT_EINVAL.  A plan in
+// JT_MODE_TC_SPLIT runs the same tensor-core kernels as jt_execute_device.
+//
+// Errors: a kernel whose bounded wait gave up raises the library's device
+// error flag; the caller learns of it from jt_check_error (after its own
+// synchronisation) or jt_synchronize.
 //
 // Sharing: every call uses the same array.  Nothing in it has to start at
 // zero (each transform writes its scratch before reading it), but two calls
@@ -1955,6 +2061,7 @@ static int noalloc_run(jt_plan *p, int op, const void *in, void *out, int64_t ba
         ar.cap = JT_NOALLOC_SCRATCH_BYTES;
         Ctx c;
         c.s = s;
+        c.tc = p->mode == JT_MODE_TC_SPLIT;  // the same kernels as jt_execute_device
         c.ws = &ar;
         c.dry = true;  // size check first: nothing may spill past the array
         JT_TRY(f->exec(c, src + b * n, n, dst + b * n, n, cb, sign, sc));
@@ -1974,6 +2081,10 @@ extern "C" int jt_execute_device_noalloc(jt_plan *p, int op, const void *dev_in,
     if (batch == 0) return JT_OK;
     const size_t esz = p->prec == JT_FLOAT32 ? 8 : 16;
     if (((uintptr_t)dev_in % esz) || ((uintptr_t)dev_out % esz)) return JT_EINVAL;
+    // the plan's tables live on the device it was created on
+    int dev = 0;
+    JT_CU(cudaGetDevice(&dev));
+    if (dev != p->device) return JT_EINVAL;
     if (p->prec == JT_FLOAT32) return noalloc_run<float>(p, op, dev_in, dev_out, batch, scale, (cudaStream_t)stream);
     return noalloc_run<double>(p, op, dev_in, dev_out, batch, scale, (cudaStream_t)stream);
 }

@@ -2,7 +2,7 @@
 resources (src/test/resources/fftw{n}.in/.out: raw little-endian complex128,
 forward DFT computed by FFTW, read by fft/DoubleFFT_1DTest.java:156-206).
 
-Run in a checkout that has the reference at REFERENCE_ROOT (argument 1).
+Run with the reference checkout as argument 1, or in JTRANSFORMS_REFERENCE.
 Sizes up to 10158 are stored (they cover every plan of the reference:
 power of two, mixed radix with radices 3, 5, 7, 11, 13 and 31, and Bluestein
 at 10158 = 2*3*1693); the larger files are only read when the reference is
@@ -32,4 +32,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("JTRANSFORMS_REFERENCE")
+    if not root:
+        sys.exit("usage: make_golden.py <JTransforms checkout> (or set JTRANSFORMS_REFERENCE)")
+    main(root)
