@@ -667,6 +667,44 @@ def run_ours(args, world, rank, local):
     return 0
 
 
+def profile_case(case: str) -> int:
+    """A small workload for ncu captures: three calls of one transform, then
+    (c1) the CUDA-core FMA peaks.  Prints what it ran."""
+    import torch
+    import jtransforms_gb300 as J
+    from jtransforms_gb300 import _native as N
+    rng = np.random.default_rng(SEED)
+    if case == "c1":
+        n, B = 4096, 256
+        plan = J.DoubleFFT_1D(n).plan
+        x = torch.from_numpy(rng.uniform(-1, 1, 2 * n * B)).cuda()
+        run = lambda: plan.execute(N.COMPLEX_FORWARD, x, 0, False, batch=B, dist=2 * n)  # noqa: E731
+    elif case == "c2b":
+        plan = J.DoubleDCT_2D(1024, 1024).plan
+        x = torch.from_numpy(blob_image(1024, rng).ravel()).cuda()
+        run = lambda: plan.execute(N.FORWARD, x, 0, True)  # noqa: E731
+    elif case == "c3b":
+        plan = J.DoubleDST_3D(128, 128, 128).plan
+        x = torch.from_numpy(rng.uniform(-1, 1, 128 ** 3)).cuda()
+        run = lambda: plan.execute(N.FORWARD, x, 0, True)  # noqa: E731
+    else:  # tc1024: the split tensor-core mode, 2^10 x 2^15 (256 MiB)
+        n, B = 1024, 1 << 15
+        plan = J.FloatFFT_1D(n).plan
+        plan.set_mode(N.MODE_TC_SPLIT)
+        x = torch.randn(2 * n * B, dtype=torch.float32, device="cuda")
+        run = lambda: plan.execute(N.COMPLEX_FORWARD, x, 0, False, batch=B, dist=2 * n)  # noqa: E731
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    if case == "c1":
+        for p, name in ((N.FLOAT64, "fp64"), (N.FLOAT32, "fp32")):
+            v = ctypes.c_double()
+            rc = N.load().jt_fma_peak(p, ctypes.byref(v))
+            print(f"fma peak {name}: rc {rc}, {v.value:.1f} GFLOP/s")
+    print(f"case {case}: 3 calls done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -683,6 +721,8 @@ def main():
     ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 1024)")
     ap.add_argument("--host-piece-mb", type=int, default=0, help="MiB per piece of the end-to-end host batch (library default 64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
+    ap.add_argument("--case", default="", choices=["", "c1", "c2b", "c3b", "tc1024"],
+                    help="profiling case: run one small workload a few times and exit (no JSON line)")
     args = ap.parse_args()
     global ELEMS, SIZES
     if args.small:
@@ -693,6 +733,8 @@ def main():
         SIZES = [int(s) for s in args.sizes.split(",")]
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup(args)
+    if args.case:
+        return profile_case(args.case)
     if args.impl == "reference":
         return run_reference(args, world, rank)
     return run_ours(args, world, rank, local)

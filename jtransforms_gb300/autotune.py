@@ -1,20 +1,23 @@
-"""Autotuner for the pass split of large power-of-two Float32 lengths.
+"""Autotuner for the pass split of large power-of-two lengths, Float32 and
+Float64.
 
 For every length 2^lo .. 2^hi it times complexForward over a device batch of
 `--mib` MiB (default 1024, the size class of the headline workload) for each
 candidate split:
 
-* one pass (lengths the register kernel holds, up to 2^14);
+* one pass (lengths the register kernel holds: up to 2^14 for float, 2^13
+  for double);
 * two passes 2^a x 2^b (column pass A, transposing row pass B), a, b <= 12;
 * three passes 2^a x 2^b x 2^c, each 4..10.
 
 Each candidate is installed with jt_set_split before its plan is created.
 Times are CUDA-event medians on the current stream after warm-up, with L2
-flushed before every call. The fastest split per length goes into
-`jt_plan_table.h`, which the library compiles in. All measurements go to
-`plan_table_f32.json` beside it.
+flushed before every call. The fastest split per length and precision goes
+into `jt_plan_table.h`, which the library compiles in (a precision that was
+not tuned keeps its current table rows). All measurements go to
+`plan_table_f32.json` / `plan_table_f64.json` beside it.
 
-    python -m jtransforms_gb300.autotune [--lo 11] [--hi 26] [--mib 1024] [--out-dir DIR]
+    python -m jtransforms_gb300.autotune [--prec f32|f64|both] [--lo 11] [--hi 26] [--mib 1024] [--out-dir DIR]
 """
 from __future__ import annotations
 
@@ -27,13 +30,15 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def candidates(lg: int):
+def candidates(lg: int, prec: str = "f32"):
     out = []
-    if lg <= 14:
+    if lg <= (14 if prec == "f32" else 13):
         out.append((0, 0, 0))
     for a in range(max(4, lg - 12), min(12, lg - 4) + 1):
         out.append((a, lg - a, 0))
-    if lg >= 14:
+    # three passes only where two can lose (they measured slower below 2^20
+    # for float; double lengths start the search at 2^18)
+    if lg >= (14 if prec == "f32" else 18):
         for a in range(4, 11):
             for b in range(4, 11):
                 c = lg - a - b
@@ -42,17 +47,19 @@ def candidates(lg: int):
     return out
 
 
-def time_split(N, J, torch, lg, split, mib, steps, warmup, flush):
+def time_split(N, J, torch, lg, split, mib, steps, warmup, flush, prec="f32"):
     n = 1 << lg
-    rc = N.load().jt_set_split(N.FLOAT32, lg, *split)
+    P = N.FLOAT32 if prec == "f32" else N.FLOAT64
+    esz = 8 if prec == "f32" else 16
+    rc = N.load().jt_set_split(P, lg, *split)
     if rc != N.OK:
         return None
     try:
-        f = J.FloatFFT_1D(n)
+        f = (J.FloatFFT_1D if prec == "f32" else J.DoubleFFT_1D)(n)
     finally:
-        N.load().jt_set_split(N.FLOAT32, lg, -1, 0, 0)
-    batch = max(1, (mib << 20) // (8 * n))
-    x = torch.randn(2 * n * batch, device="cuda", dtype=torch.float32)
+        N.load().jt_set_split(P, lg, -1, 0, 0)
+    batch = max(1, (mib << 20) // (esz * n))
+    x = torch.randn(2 * n * batch, device="cuda", dtype=torch.float32 if prec == "f32" else torch.float64)
     stream = torch.cuda.current_stream()
     times = []
     for s in range(warmup + steps):
@@ -67,29 +74,46 @@ def time_split(N, J, torch, lg, split, mib, steps, warmup, flush):
     ms = statistics.median(a.elapsed_time(b) for a, b in times)
     algo = f.plan.algorithm(0)
     del f, x
-    return {"ms": ms, "GB/s": 2 * 8 * n * batch / (ms * 1e-3) / 1e9, "batch": batch, "algorithm": algo}
+    return {"ms": ms, "GB/s": 2 * esz * n * batch / (ms * 1e-3) / 1e9, "batch": batch, "algorithm": algo}
+
+
+def read_header(path: str) -> dict:
+    """The rows of the current table per precision, {prec: {lg: split}}."""
+    import re
+    out = {"f32": {}, "f64": {}}
+    if not os.path.exists(path):
+        return out
+    text = open(path).read()
+    for prec, name in (("f32", "kSplitF32"), ("f64", "kSplitF64")):
+        m = re.search(name + r"\[31\]\[3\] = \{(.*?)\};", text, re.S)
+        if not m:
+            continue
+        rows = re.findall(r"\{(-?\d+), (-?\d+), (-?\d+)\}", m.group(1))
+        for lg, r in enumerate(rows):
+            if int(r[0]) >= 0:
+                out[prec][lg] = tuple(int(v) for v in r)
+    return out
 
 
 def write_header(best: dict, path: str):
-    rows = []
-    for lg in range(31):
-        s = best.get(lg)
-        rows.append("{%d, %d, %d}" % tuple(s) if s is not None else "{-1, -1, -1}")
-    none = ", ".join(["{-1, -1, -1}"] * 31)
-    body = ",\n    ".join(", ".join(rows[i:i + 8]) for i in range(0, 31, 8))
+    """best: {prec: {lg: split}}."""
+    def body(tab):
+        rows = ["{%d, %d, %d}" % tuple(tab[lg]) if lg in tab else "{-1, -1, -1}" for lg in range(31)]
+        return ",\n    ".join(", ".join(rows[i:i + 8]) for i in range(0, 31, 8))
     with open(path, "w") as fh:
         fh.write("// jt_plan_table.h -- pass split per power-of-two length, indexed by log2 n:\n"
                  "// {0,0,0} one pass, {a,b,0} two passes 2^a (column) x 2^b (row), {a,b,c}\n"
                  "// three passes, {-1,-1,-1} no entry (the engine's rules decide).\n"
                  "// Regenerated by `python -m jtransforms_gb300.autotune` on the target GPU;\n"
-                 "// the measurements are in plan_table_f32.json.\n"
+                 "// the measurements are in plan_table_f32.json and plan_table_f64.json.\n"
                  "#pragma once\n\n"
-                 "static const signed char kSplitF32[31][3] = {\n    " + body + ",\n};\n\n"
-                 "static const signed char kSplitF64[31][3] = {\n    " + none + ",\n};\n")
+                 "static const signed char kSplitF32[31][3] = {\n    " + body(best["f32"]) + ",\n};\n\n"
+                 "static const signed char kSplitF64[31][3] = {\n    " + body(best["f64"]) + ",\n};\n")
 
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
+    ap.add_argument("--prec", choices=["f32", "f64", "both"], default="both")
     ap.add_argument("--lo", type=int, default=11)
     ap.add_argument("--hi", type=int, default=26)
     ap.add_argument("--mib", type=int, default=1024)
@@ -109,24 +133,33 @@ def main(argv=None) -> int:
     def flush():
         flushbuf.fill_(1.0)
 
-    results, best = {}, {}
-    for lg in range(args.lo, args.hi + 1):
-        res = {}
-        for sp in candidates(lg):
-            r = time_split(N, J, torch, lg, sp, args.mib, args.steps, args.warmup, flush)
-            if r is not None:
-                res["%d,%d,%d" % sp] = r
-        if not res:
-            continue
-        key = min(res, key=lambda k: res[k]["ms"])
-        best[lg] = tuple(int(v) for v in key.split(","))
-        results[lg] = {"best": key, "candidates": res}
-        print(f"2^{lg}: best {key} {res[key]['GB/s']:.0f} GB/s", flush=True)
     out_dir = args.out_dir or os.path.join(HERE, "csrc")
     os.makedirs(out_dir, exist_ok=True)
-    write_header(best, os.path.join(out_dir, "jt_plan_table.h"))
-    with open(os.path.join(args.out_dir or HERE, "plan_table_f32.json"), "w") as fh:
-        json.dump({"device": torch.cuda.get_device_name(0), "mib_per_call": args.mib, "sizes": results}, fh, indent=1)
+    header = os.path.join(out_dir, "jt_plan_table.h")
+    best = read_header(os.path.join(HERE, "csrc", "jt_plan_table.h"))
+    for prec in (["f32", "f64"] if args.prec == "both" else [args.prec]):
+        results = {}
+        best[prec] = {}
+        for lg in range(args.lo, args.hi + 1):
+            res = {}
+            for sp in candidates(lg, prec):
+                try:
+                    r = time_split(N, J, torch, lg, sp, args.mib, args.steps, args.warmup, flush, prec)
+                except (N.IllegalArgumentException, N.IllegalStateException) as e:
+                    print(f"{prec} 2^{lg} {sp}: skipped ({e})", flush=True)
+                    r = None
+                if r is not None:
+                    res["%d,%d,%d" % sp] = r
+            if not res:
+                continue
+            key = min(res, key=lambda k: res[k]["ms"])
+            best[prec][lg] = tuple(int(v) for v in key.split(","))
+            results[lg] = {"best": key, "candidates": res}
+            print(f"{prec} 2^{lg}: best {key} {res[key]['GB/s']:.0f} GB/s", flush=True)
+        with open(os.path.join(args.out_dir or HERE, f"plan_table_{prec}.json"), "w") as fh:
+            json.dump({"device": torch.cuda.get_device_name(0), "mib_per_call": args.mib, "sizes": results}, fh,
+                      indent=1)
+    write_header(best, header)
     return 0
 
 

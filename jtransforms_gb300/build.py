@@ -16,7 +16,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "libjtgpu.so")
 BUILD = os.path.join(PKG, "_build")
-SOURCES = ["jt_engine.cu", "jt_pow2_f32.cu", "jt_pow2_f64.cu", "jt_tc_f32.cu", "jt_peak.cu"]
+SOURCES = ["jt_engine.cu", "jt_pow2_f32.cu", "jt_pow2_f64.cu", "jt_tc_f32.cu", "jt_peak.cu", "jt_r2r_f32.cu",
+           "jt_r2r_f64.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + os.path.join(ROOT, "include")]

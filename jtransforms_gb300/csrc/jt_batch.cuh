@@ -16,10 +16,11 @@
 
 #include "jt_device.cuh"
 #include "jt_stockham.cuh"
+#include "jt_r2r.cuh"
 
 namespace jt {
 
-enum BOpType { BOP_TILE = 0, BOP_STOCK = 1, BOP_ELEM = 2 };
+enum BOpType { BOP_TILE = 0, BOP_STOCK = 1, BOP_ELEM = 2, BOP_R2R = 3 };
 
 enum ElemKind {
     EK_COPY_COMPLEX = 0,
@@ -57,6 +58,7 @@ struct BOp {
     // tile / stock
     TileParams tp;
     StockParams sp;
+    R2rParams rp;  // DCT/DST/DHT lines in one step (kind: the R2rOp)
     const void *in;
     void *out;
     const void *W, *Whi, *Wlo;
@@ -138,6 +140,16 @@ template <typename T> __device__ void elem_dispatch(const BOp &o, int64_t idx) {
     }
 }
 
+template <typename T> __device__ void r2r_dispatch(const BOp &o, int idx, unsigned char *smem) {
+    typedef typename V2<T>::t C2;
+    const T *in = (const T *)o.in;
+    T *out = (T *)o.out;
+    const C2 *W = (const C2 *)o.W, *Wr = (const C2 *)o.Whi, *Wd = (const C2 *)o.Wlo;
+    if (o.kind == R2R_DCT2) r2r_tile_body<R2R_DCT2, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
+    else if (o.kind == R2R_DCT3) r2r_tile_body<R2R_DCT3, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
+    else r2r_tile_body<R2R_DHT, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
+}
+
 __device__ __forceinline__ int ld_acquire_gpu(const int *p) {
     int v;
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -186,6 +198,9 @@ __global__ void __launch_bounds__(JT_BATCH_THREADS, 1)
                     if (o.sign < 0) tile_fft_body<-1, double>((const double2 *)o.in, (double2 *)o.out, o.tp, (const double2 *)o.W, (const double2 *)o.Whi, (const double2 *)o.Wlo, tk.idx, smem_raw);
                     else tile_fft_body<1, double>((const double2 *)o.in, (double2 *)o.out, o.tp, (const double2 *)o.W, (const double2 *)o.Whi, (const double2 *)o.Wlo, tk.idx, smem_raw);
                 }
+            } else if (o.type == BOP_R2R) {
+                if (o.prec == 0) r2r_dispatch<float>(o, tk.idx, smem_raw);
+                else r2r_dispatch<double>(o, tk.idx, smem_raw);
             } else if (o.type == BOP_STOCK) {
                 // one power-of-two double line of 8192 (too long for the tile kernel)
                 if (o.sign < 0) stockham_body<double, 8192, 0, -1>((const double2 *)o.in, (double2 *)o.out, o.sp, (const double2 *)o.W, nullptr, nullptr, tk.idx, smem_raw);

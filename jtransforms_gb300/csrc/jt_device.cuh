@@ -323,6 +323,32 @@ __device__ void pass_generic(const C2 *__restrict__ src, C2 *__restrict__ dst, i
     }
 }
 
+// The Stockham passes of a tile: `lines` lines of length L at stride Lp in
+// `src`, ping-ponging with `dst`; returns the buffer holding the result.
+template <int SIGN, typename T>
+__device__ C2 *tile_passes(C2 *src, C2 *dst, int lines, int L, int Lp, int npass, const int *radix, const C2 *__restrict__ W) {
+    int Ns = 1;
+    for (int ps = 0; ps < npass; ps++) {
+        const int R = radix[ps];
+        switch (R) {
+            case 2: pass_r<2, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
+            case 3: pass_r<3, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
+            case 4: pass_r<4, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
+            case 5: pass_r<5, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
+            case 7: pass_r<7, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
+            case 8: pass_r<8, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
+            case 16: pass_r<16, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
+            default: pass_generic<SIGN, T>(src, dst, lines, L, Lp, Ns, R, W); break;
+        }
+        __syncthreads();
+        C2 *t = src;
+        src = dst;
+        dst = t;
+        Ns *= R;
+    }
+    return src;
+}
+
 // W: e^{-2 pi i t/L}, t < L.  Whi/Wlo: two-level table of the four-step post
 // twiddle, e^{-2 pi i t/tw_n} = Whi[t >> lo_bits] * Wlo[t & mask].
 // Tile `blk` of a generic line pass, run by the calling CTA with its shared
@@ -353,26 +379,7 @@ __device__ void tile_fft_body(const C2 *in, C2 *out, const TileParams &p, const 
     }
     __syncthreads();
 
-    C2 *src = bufA, *dst = bufB;
-    int Ns = 1;
-    for (int ps = 0; ps < p.npass; ps++) {
-        const int R = p.radix[ps];
-        switch (R) {
-            case 2: pass_r<2, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
-            case 3: pass_r<3, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
-            case 4: pass_r<4, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
-            case 5: pass_r<5, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
-            case 7: pass_r<7, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
-            case 8: pass_r<8, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
-            case 16: pass_r<16, SIGN, T>(src, dst, lines, L, Lp, Ns, W); break;
-            default: pass_generic<SIGN, T>(src, dst, lines, L, Lp, Ns, R, W); break;
-        }
-        __syncthreads();
-        C2 *t = src;
-        src = dst;
-        dst = t;
-        Ns *= R;
-    }
+    const C2 *src = tile_passes<SIGN, T>(bufA, bufB, lines, L, Lp, p.npass, p.radix, W);
 
     T sc;
     if constexpr (sizeof(T) == 4) sc = p.scalef;

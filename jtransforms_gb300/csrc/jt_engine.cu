@@ -16,6 +16,7 @@
 #include "jt_device.cuh"
 #include "jt_stockham.cuh"
 #include "jt_batch.cuh"
+#include "jt_r2r.cuh"
 #include "jt_plan_table.h"
 #include "../../include/jtgpu.h"
 
@@ -32,6 +33,7 @@
 #include <new>
 #include <string>
 #include <tuple>
+#include <thread>
 #include <vector>
 
 namespace jt {
@@ -184,6 +186,12 @@ static int device_init() {
         cudaFuncSetAttribute(fft_tile_kernel<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(fft_tile_kernel<-1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(fft_tile_kernel<1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT3, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_DHT, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT3, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_DHT, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         if (cudaGetLastError() != cudaSuccess) g_dev_status = JT_ECUDA;
     });
     return g_dev_status;
@@ -199,6 +207,13 @@ bool stockham_pipe_ok(int L, int mode, const double *);
 int stockham_lines_per_cta(int L, int mode, const float *);
 int stockham_lines_per_cta(int L, int mode, const double *);
 bool tc_split_ok(int L);
+// Register-form DCT/DST/DHT lines (jt_r2r_f32.cu, jt_r2r_f64.cu).
+bool r2r_reg_launch(int H, int op, const float *in, float *out, const R2rParams &p, const float2 *Wp, const float2 *Wr,
+                    const float2 *Wd, cudaStream_t s);
+bool r2r_reg_launch(int H, int op, const double *in, double *out, const R2rParams &p, const double2 *Wp, const double2 *Wr,
+                    const double2 *Wd, cudaStream_t s);
+int r2r_reg_lines(int H, const float *);
+int r2r_reg_lines(int H, const double *);
 bool tc_split_launch(int L, int sign, const float2 *in, float2 *out, const StockParams &p, const float2 *W, int *err, int sms,
                      cudaStream_t s);
 
@@ -944,6 +959,109 @@ template <typename T> struct Real1 {
 };
 
 // ---------------------------------------------------------------------------
+// One-kernel DCT/DST/DHT lines (jt_r2r.cuh): even n whose half length the
+// tile passes run (h = n/2 up to the tile kernel's limit, prime factors <= 63),
+// any line layout.  Batch recordings keep the separate pre/post steps.
+// ---------------------------------------------------------------------------
+template <typename T> static bool r2r_fused_ok(const Ctx &, int64_t n, const Real1<T> *rf) {
+    return n >= 4 && n % 2 == 0 && rf && rf->half && rf->half->algo == ALG_DIRECT && rf->half->W && rf->Wr &&
+           Fft1<T>::generic_ok(n / 2);
+}
+
+// Lines per CTA of the register form for half length h (0: none): power-of-
+// two h from 16 to 4096 whose plan holds the pass table
+template <typename T> static int r2r_reg_c(int64_t h, const Real1<T> *rf) {
+    if (!is_pow2(h) || h < 16 || h > 4096 || !rf->half->reg || !rf->half->Wp) return 0;
+    return r2r_reg_lines((int)h, (const T *)nullptr);
+}
+
+// Whether strided (column) lines run in one kernel with coalesced enough
+// access: at least 32-byte runs of adjacent lines per CTA
+template <typename T> static bool r2r_strided_ok(const Ctx &ctx, int64_t n, const Real1<T> *rf) {
+    if (!r2r_fused_ok<T>(ctx, n, rf)) return false;
+    const int64_t h = n / 2;
+    const int need = (int)(32 / sizeof(T));
+    if (r2r_reg_c<T>(h, rf) >= need) return true;
+    const size_t per_line = 2 * (size_t)padded_len((int)h) * sizeof(typename V2<T>::t);
+    return (size_t)g_smem_optin / per_line >= (size_t)need;
+}
+
+template <typename T>
+static int r2r_fused(Ctx &ctx, int op, const Real1<T> *rf, const T *in, T *out, int64_t nlines, const Layout &lin,
+                     const Layout &lout, int dst, double mult, double mult0, const typename V2<T>::t *Wd) {
+    typedef typename V2<T>::t C2;
+    if (nlines <= 0) return JT_OK;
+    const int64_t n = rf->n, h = n / 2;
+    std::vector<int> rr = direct_radices(h);
+    if (rr.empty() || (int)rr.size() > JT_MAX_PASSES) return JT_EINVAL;
+    R2rParams p;
+    memset(&p, 0, sizeof(p));
+    p.n = (int)n;
+    p.npass = (int)rr.size();
+    for (int i = 0; i < p.npass; i++) p.radix[i] = rr[i];
+    const int Lp = padded_len((int)h);
+    const bool strided = lin.estride != 1 || lout.estride != 1;
+    int C = (int)std::max<int64_t>(1, (sizeof(T) == 4 ? 4096 : 2048) / h);
+    if (strided) C = std::max(C, sizeof(T) == 4 ? 16 : 8);
+    const size_t per_line = 2 * (size_t)Lp * sizeof(C2);
+    C = std::min(C, (int)std::max<size_t>(1, (size_t)g_smem_optin / per_line));
+    if ((int64_t)C > nlines) C = (int)nlines;
+    p.C = C;
+    p.nlines = nlines;
+    p.lin = lin;
+    p.lout = lout;
+    p.dst = dst;
+    p.mult = mult;
+    p.mult0 = mult0;
+    p.multf = (float)mult;
+    p.mult0f = (float)mult0;
+    if (ctx.rec) {
+        // a batch step: the tile form, run by the batch kernel's CTAs
+        BOp o;
+        memset(&o, 0, sizeof(o));
+        o.type = BOP_R2R;
+        o.prec = sizeof(T) == 4 ? 0 : 1;
+        o.kind = op;
+        o.in = in;
+        o.out = out;
+        o.W = rf->half->W;
+        o.Whi = rf->Wr;
+        o.Wlo = Wd;
+        o.rp = p;
+        o.ntasks = (int)cdiv(nlines, C);
+        o.smem = (int)(per_line * C);
+        emit(ctx, o);
+        return JT_OK;
+    }
+    // the register form when h has one and the runs stay coalesced; lines
+    // per CTA from its maximum down so that the grid covers the SMs twice
+    // (at least 32-byte runs on strided lines, at least one warp per CTA)
+    const int creg = r2r_reg_c<T>(h, rf);
+    if (creg > 0 && (!strided || creg >= (int)(32 / sizeof(T)))) {
+        int cr = creg;
+        const int cmin = std::max<int>(strided ? (int)(32 / sizeof(T)) : 1, (int)std::max<int64_t>(1, 32 / (h / 16)));
+        while (cr > cmin && cdiv(nlines, cr) < 2 * (int64_t)g_sms) cr /= 2;
+        p.C = std::max(cr, 1);
+        if (ctx.dry) return JT_OK;
+        if (cdiv(nlines, creg) > 0x7fffffff) return JT_ETOOBIG;
+        if (!r2r_reg_launch((int)h, op, in, out, p, rf->half->Wp, rf->Wr, Wd, ctx.s)) return JT_EINVAL;
+        g_launches++;
+        return JT_OK;
+    }
+    if (ctx.dry) return JT_OK;
+    const int64_t grid = cdiv(nlines, C);
+    if (grid > 0x7fffffff) return JT_ETOOBIG;
+    const int threads = (int)std::min<int64_t>(512, std::max<int64_t>(64, cdiv((int64_t)C * h / 8, 32) * 32));
+    const size_t smem = per_line * C;
+    const C2 *W = rf->half->W;
+    if (op == R2R_DCT2) r2r_tile_kernel<R2R_DCT2, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
+    else if (op == R2R_DCT3) r2r_tile_kernel<R2R_DCT3, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
+    else r2r_tile_kernel<R2R_DHT, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
+    g_launches++;
+    return JT_OK;
+}
+
+// ---------------------------------------------------------------------------
 // DCT-II/III and DST-II/III (dct/DoubleDCT_1D.java:169-440, dst/DoubleDST_1D.java)
 // ---------------------------------------------------------------------------
 template <typename T> struct Dct1 {
@@ -966,6 +1084,40 @@ template <typename T> struct Dct1 {
         return JT_OK;
     }
     int64_t vdist() const { return (n + 1) & ~(int64_t)1; }
+
+    bool strided_ok(const Ctx &ctx) const { return r2r_strided_ok<T>(ctx, n, rf.get()); }
+
+    // `nlines` lines in place with layout l (scalar units): one kernel when
+    // the length allows it, else (contiguous lines only) the separate steps
+    int lines(Ctx &ctx, bool fwd, T *a, int64_t nlines, const Layout &l, bool scale, bool dst) const {
+        if (n == 1 || nlines <= 0) return JT_OK;
+        if (r2r_fused_ok<T>(ctx, n, rf.get())) {
+            double m, m0;
+            if (fwd) {
+                if (scale) {
+                    m = std::sqrt(2.0 / (double)n);
+                    m0 = 1.0 / std::sqrt((double)n);
+                } else {
+                    m = m0 = is_pow2(n) ? 1.0 : 2.0;
+                }
+                return r2r_fused<T>(ctx, R2R_DCT2, rf.get(), a, a, nlines, l, l, dst, m, m0, Wd);
+            }
+            // coefficient scales of the inverse: q for k >= 1, 2 q0 for k = 0
+            if (scale) {
+                m = std::sqrt(2.0 / (double)n);
+                m0 = 2.0 / std::sqrt((double)n);
+            } else if (is_pow2(n)) {
+                m = 1.0;
+                m0 = 2.0;
+            } else {
+                m = 1.0 / (double)n;
+                m0 = 1.0 / (double)n;
+            }
+            return r2r_fused<T>(ctx, R2R_DCT3, rf.get(), a, a, nlines, l, l, dst, m, m0, Wd);
+        }
+        if (l.estride != 1 || (l.inner != 1 && nlines > 1)) return JT_EINVAL;
+        return fwd ? forward(ctx, a, l.outer, nlines, scale, dst) : inverse(ctx, a, l.outer, nlines, scale, dst);
+    }
 
     int forward(Ctx &ctx, T *a, int64_t dist, int64_t batch, bool scale, bool dst) const {
         if (n == 1 || batch <= 0) return JT_OK;
@@ -1036,6 +1188,16 @@ template <typename T> struct Dht1 {
         out = std::move(d);
         return JT_OK;
     }
+    bool strided_ok(const Ctx &ctx) const { return r2r_strided_ok<T>(ctx, n, rf.get()); }
+
+    // `nlines` lines in place with layout l (scalar units)
+    int lines(Ctx &ctx, T *a, int64_t nlines, const Layout &l, double mult) const {
+        if (n == 1 || nlines <= 0) return JT_OK;
+        if (r2r_fused_ok<T>(ctx, n, rf.get())) return r2r_fused<T>(ctx, R2R_DHT, rf.get(), a, a, nlines, l, l, 0, mult, mult, nullptr);
+        if (l.estride != 1 || (l.inner != 1 && nlines > 1)) return JT_EINVAL;
+        return forward(ctx, a, l.outer, nlines, mult);
+    }
+
     int forward(Ctx &ctx, T *a, int64_t dist, int64_t batch, double mult) const {
         if (n == 1 || batch <= 0) return JT_OK;
         const int64_t vd = (n + 1) & ~(int64_t)1;
@@ -1164,17 +1326,22 @@ template <typename T> struct PlanImpl {
         return JT_OK;
     }
 
-    // Applies a real 1D line operation along every axis (DCT/DST/DHT).
-    template <typename F> int real_axes(Ctx &ctx, T *a, int64_t batch, F line_op) {
+    // Applies a real 1D line operation along every axis (DCT/DST/DHT):
+    // line_op(ctx, len, array, nlines, layout).  Strided axes run in place
+    // when the length has the one-kernel form (strided_ok(len)), else
+    // through a transposed copy.
+    template <typename F, typename G> int real_axes(Ctx &ctx, T *a, int64_t batch, F line_op, G strided_ok) {
         for (int ax = nd - 1; ax >= 0; ax--) {
             int64_t outer, len, inner;
             axis_shape(ax, batch, outer, len, inner);
             if (inner == 1) {
-                JT_TRY(line_op(ctx, len, a, len, outer));
+                JT_TRY(line_op(ctx, len, a, outer, Layout{1, len, 0, 1}));
+            } else if (strided_ok(len)) {
+                JT_TRY(line_op(ctx, len, a, outer * inner, Layout{inner, len * inner, 1, inner}));
             } else {
                 T *tmp = (T *)ctx.ws->get(sizeof(T) * outer * len * inner, ctx.dry);
                 transpose<T>(ctx, a, tmp, outer, len, inner);
-                JT_TRY(line_op(ctx, len, tmp, len, outer * inner));
+                JT_TRY(line_op(ctx, len, tmp, outer * inner, Layout{1, len, 0, 1}));
                 transpose<T>(ctx, tmp, a, outer, inner, len);
             }
         }
@@ -1276,22 +1443,25 @@ template <typename T> struct PlanImpl {
             const bool dst = kind == JT_DST;
             if (nd == 1) {
                 Dct1<T> *d = dct.at(dims[0]).get();
-                return fwd ? d->forward(ctx, a, dist, batch, scale, dst) : d->inverse(ctx, a, dist, batch, scale, dst);
+                return d->lines(ctx, fwd, a, batch, Layout{1, dist, 0, 1}, scale, dst);
             }
-            return real_axes(ctx, a, batch, [&](Ctx &c, int64_t len, T *x, int64_t xd, int64_t nb) {
-                Dct1<T> *d = dct.at(len).get();
-                return fwd ? d->forward(c, x, xd, nb, scale, dst) : d->inverse(c, x, xd, nb, scale, dst);
-            });
+            return real_axes(
+                ctx, a, batch,
+                [&](Ctx &c, int64_t len, T *x, int64_t nb, const Layout &l) {
+                    return dct.at(len)->lines(c, fwd, x, nb, l, scale, dst);
+                },
+                [&](int64_t len) { return dct.at(len)->strided_ok(ctx); });
         }
         // DHT
         if (nd == 1) {
             Dht1<T> *h = dht.at(dims[0]).get();
             double mult = (!fwd && scale) ? 1.0 / (double)dims[0] : 1.0;
-            return h->forward(ctx, a, dist, batch, mult);
+            return h->lines(ctx, a, batch, Layout{1, dist, 0, 1}, mult);
         }
-        JT_TRY(real_axes(ctx, a, batch, [&](Ctx &c, int64_t len, T *x, int64_t xd, int64_t nb) {
-            return dht.at(len)->forward(c, x, xd, nb, 1.0);
-        }));
+        JT_TRY(real_axes(
+            ctx, a, batch,
+            [&](Ctx &c, int64_t len, T *x, int64_t nb, const Layout &l) { return dht.at(len)->lines(c, x, nb, l, 1.0); },
+            [&](int64_t len) { return dht.at(len)->strided_ok(ctx); }));
         for (int64_t b = 0; b < batch; b++) {
             T *p = a + b * dist;
             if (nd == 2) LAUNCH1D(ctx, (dims[0] / 2 + 1) * (dims[1] / 2 + 1), ytransform2_kernel<T>, p, dims[0], dims[1]);
@@ -1447,6 +1617,125 @@ int check_op(const jt_plan *p, int op) {
     return JT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Host-staged four-step: one complex 1D transform whose device working set
+// does not fit the device budget (the free device memory, or
+// JT_OPT_ARENA_LIMIT_MB) runs as n = n1 x m over host pieces, the way the
+// reference's LargeArray path works through its array in parts
+// (fft/DoubleFFT_1D.java:280-304):
+//   pass A  blocks of w columns of the n1 x m view: copied in as n1 x w
+//           (one 2D copy), n1-point column FFTs, the four-step twiddle
+//           w_n^{k1 (b0 + c)}, copied back in place;
+//   pass B  blocks of h rows: copied in, m-point row FFTs (scaled for the
+//           inverse), transposed on the device and written to
+//           X[k1 + n1 k2] of a host copy, which replaces the array at the end.
+// Device memory: two block buffers and the row plan's scratch.
+// ---------------------------------------------------------------------------
+template <int SIGN, typename T>
+__global__ void block_twiddle_kernel(typename V2<T>::t *y, int64_t n1, int64_t w, int64_t b0, int64_t n,
+                                     const typename V2<T>::t *__restrict__ Whi, const typename V2<T>::t *__restrict__ Wlo,
+                                     int lo_bits) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n1 * w) return;
+    const int64_t k1 = i / w, c = i - k1 * w;
+    const uint64_t e = ((uint64_t)k1 * (uint64_t)(b0 + c)) % (uint64_t)n;
+    const typename V2<T>::t t = cmul<T>(Whi[e >> lo_bits], Wlo[e & ((1ull << lo_bits) - 1)]);
+    y[i] = SIGN < 0 ? cmul<T>(y[i], t) : cmulc<T>(y[i], t);
+}
+
+static int64_t device_budget() {
+    const int64_t lim = g_opt_arena_limit.load();
+    if (lim > 0) return lim;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return INT64_MAX;
+    // the arena itself can be given back and regrown
+    return (int64_t)fr + (int64_t)t_state.arena.cap - ((int64_t)256 << 20);
+}
+
+template <typename T>
+int stream_fourstep(PlanImpl<T> *im, Fft1<T> *f, void *host, int sign, double scale, int64_t budget) {
+    typedef typename V2<T>::t C2;
+    const int64_t n = f->n, n1 = f->n1, m = n / n1;
+    const int64_t esz = (int64_t)sizeof(C2);
+    if (!f->Whi || !f->pa) return JT_ENOMEM;
+    // the caller's array holds pairs of T at any T-aligned address: host
+    // addresses are formed in bytes
+    char *h = (char *)host;
+    // the m-point row plan: pass B of a two-pass plan, or (three passes) a
+    // plan of its own
+    std::shared_ptr<Fft1<T>> fm_own;
+    Fft1<T> *fm = f->algo == ALG_TWOPASS ? f->pb.get() : nullptr;
+    if (!fm) {
+        const uint64_t seq0 = g_setup_seq.load();
+        JT_TRY(cached<Fft1<T>>(m, fm_own));
+        if (g_setup_seq.load() != seq0) JT_CU(cudaStreamSynchronize(g_setup));
+        fm = fm_own.get();
+    }
+    cudaStream_t s = t_state.stream;
+    Ctx c;
+    c.s = s;
+    c.ws = &t_state.arena;
+    // block size: the largest (down to one row of m) whose working set fits
+    int64_t blk = std::min<int64_t>(budget / 3, (int64_t)256 << 20), w = 0, hr = 0;
+    for (;; blk /= 2) {
+        if (blk < m * esz) return JT_ENOMEM;  // not even one row fits
+        w = std::max<int64_t>(1, std::min<int64_t>(m, blk / (n1 * esz)));
+        hr = std::max<int64_t>(1, std::min<int64_t>(n1, blk / (m * esz)));
+        c.dry = true;
+        t_state.arena.used = t_state.arena.peak = 0;
+        t_state.arena.get(blk, true);
+        t_state.arena.get(blk, true);
+        Layout la = {w, n1 * w, 1, w};
+        JT_TRY(f->pa->exec_direct(c, nullptr, nullptr, w, la, la, sign, 1.0));
+        JT_TRY(fm->exec(c, nullptr, m, nullptr, m, hr, sign, scale));
+        if ((int64_t)t_state.arena.peak <= budget) break;
+    }
+    JT_TRY(ensure_arena(t_state.arena.peak));
+    std::unique_ptr<C2[]> out(new (std::nothrow) C2[n]);
+    if (!out) return JT_ENOMEM;
+    c.dry = false;
+    t_state.arena.used = 0;
+    C2 *d0 = (C2 *)t_state.arena.get(blk, false), *d1 = (C2 *)t_state.arena.get(blk, false);
+    const size_t mark = t_state.arena.used;
+    // pass A: column blocks, in place in the host array
+    for (int64_t b0 = 0; b0 < m; b0 += w) {
+        const int64_t wb = std::min(w, m - b0);
+        JT_CU(cudaMemcpy2DAsync(d0, wb * esz, h + b0 * esz, m * esz, wb * esz, n1, cudaMemcpyHostToDevice, s));
+        Layout la = {wb, n1 * wb, 1, wb};
+        t_state.arena.used = mark;
+        JT_TRY(f->pa->exec_direct(c, d0, d0, wb, la, la, sign, 1.0));
+        const int64_t tot = n1 * wb;
+        if (sign < 0)
+            block_twiddle_kernel<-1, T><<<(unsigned)cdiv(tot, 256), 256, 0, s>>>(d0, n1, wb, b0, n, f->Whi, f->Wlo, f->lo_bits);
+        else
+            block_twiddle_kernel<1, T><<<(unsigned)cdiv(tot, 256), 256, 0, s>>>(d0, n1, wb, b0, n, f->Whi, f->Wlo, f->lo_bits);
+        g_launches++;
+        JT_CU(cudaMemcpy2DAsync(h + b0 * esz, m * esz, d0, wb * esz, wb * esz, n1, cudaMemcpyDeviceToHost, s));
+    }
+    // pass B: row blocks, transposed into the host copy
+    for (int64_t r0 = 0; r0 < n1; r0 += hr) {
+        const int64_t hb = std::min(hr, n1 - r0);
+        JT_CU(cudaMemcpyAsync(d0, h + r0 * m * esz, hb * m * esz, cudaMemcpyHostToDevice, s));
+        t_state.arena.used = mark;
+        JT_TRY(fm->exec(c, d0, m, d0, m, hb, sign, scale));
+        im->template transpose<C2>(c, d0, d1, 1, hb, m);
+        JT_CU(cudaMemcpy2DAsync(out.get() + r0, n1 * esz, d1, hb * esz, hb * esz, m, cudaMemcpyDeviceToHost, s));
+    }
+    JT_CU(cudaStreamSynchronize(s));
+    JT_CU(cudaGetLastError());
+    JT_TRY(check_err_flag());
+    // the result replaces the array (a few threads: the copy is host-bound)
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(8, n / ((int64_t)1 << 22)));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++)
+        th.emplace_back([&, t] {
+            const int64_t a = n * t / nt, b = n * (t + 1) / nt;
+            std::memcpy(h + a * esz, out.get() + a, (size_t)(b - a) * esz);
+        });
+    for (auto &x : th) x.join();
+    return JT_OK;
+}
+
 template <typename T>
 int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t batch, int64_t dist, int scale) {
     int64_t ext = 0;
@@ -1483,6 +1772,31 @@ int exec_host(jt_plan *p, int op, void *host, int64_t len, int64_t off, int64_t 
     for (int r = 0; r < ring; r++) t_state.arena.get(per * piece, true);
     std::lock_guard<std::mutex> g(im->mu);
     JT_TRY(im->run(c, op, (T *)nullptr, piece, dd, scale != 0));
+    const int64_t budget = device_budget();
+    if ((int64_t)t_state.arena.peak > budget) {
+        // one transform's working set exceeds the device: complex 1D
+        // multi-pass lengths stream through host pieces, the rest fail
+        Fft1<T> *f = nullptr;
+        if (p->kind == JT_FFT && p->nd == 1 && (op == JT_COMPLEX_FORWARD || op == JT_COMPLEX_INVERSE)) {
+            auto it = im->fft.find(p->dims[0]);
+            if (it != im->fft.end() && (it->second->algo == ALG_TWOPASS || it->second->algo == ALG_THREEPASS))
+                f = it->second.get();
+        }
+        if (!f) {
+            g_last_cuda = (int)cudaErrorMemoryAllocation;
+            return JT_ENOMEM;
+        }
+        if (t_state.last && t_state.last != s) {
+            JT_CU(cudaEventRecord(t_state.done, t_state.last));
+            JT_CU(cudaStreamWaitEvent(s, t_state.done, 0));
+        }
+        const int sign = op == JT_COMPLEX_FORWARD ? -1 : 1;
+        const double sc = (op == JT_COMPLEX_INVERSE && scale) ? 1.0 / (double)p->dims[0] : 1.0;
+        for (int64_t b = 0; b < batch; b++)
+            JT_TRY(stream_fourstep<T>(im, f, (T *)host + off + b * dist, sign, sc, budget));
+        t_state.last = s;
+        return JT_OK;
+    }
     JT_TRY(ensure_arena(t_state.arena.peak));
     if (t_state.last && t_state.last != s) {
         JT_CU(cudaEventRecord(t_state.done, t_state.last));

@@ -100,3 +100,31 @@ def test_huge_single_tone_and_round_trip(cls, n, algo):
     assert math.sqrt(num / n) <= tol(n, npdt)
     del x, ref
     torch.cuda.empty_cache()
+
+
+def test_host_array_above_2_31_elements():
+    """jt_execute on a HOST array of 2^32 floats (2^31 complex elements, the
+    FloatLargeArray overload's range): the single tone comes out at bin k0
+    and the scaled inverse brings it back."""
+    import torch
+
+    import jtransforms_gb300 as J
+    n = 1 << 31
+    f = J.FloatFFT_1D(n)
+    k0 = 987654321 % n
+    host = _tone(n, k0, torch.float32).cpu().numpy()
+    assert host.size == 1 << 32
+    f.complexForward(host)
+    y = torch.from_numpy(host).cuda()
+    assert _tone_error(y, n, k0) <= tol(n, np.float32)
+    del y
+    f.complexInverse(host, True)
+    back = torch.from_numpy(host).cuda()
+    ref = _tone(n, k0, torch.float32)
+    num = 0.0
+    step = 1 << 28
+    for i0 in range(0, 2 * n, step):
+        num += float(torch.sum((back[i0:i0 + step].to(torch.float64) - ref[i0:i0 + step].to(torch.float64)) ** 2))
+    assert math.sqrt(num / n) <= tol(n, np.float32)
+    del back, ref, host
+    torch.cuda.empty_cache()
