@@ -147,7 +147,9 @@ template <typename T> __device__ void r2r_dispatch(const BOp &o, int idx, unsign
     const C2 *W = (const C2 *)o.W, *Wr = (const C2 *)o.Whi, *Wd = (const C2 *)o.Wlo;
     if (o.kind == R2R_DCT2) r2r_tile_body<R2R_DCT2, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
     else if (o.kind == R2R_DCT3) r2r_tile_body<R2R_DCT3, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
-    else r2r_tile_body<R2R_DHT, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
+    else if (o.kind == R2R_DHT) r2r_tile_body<R2R_DHT, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
+    else if (o.kind == R2R_RFWD) r2r_tile_body<R2R_RFWD, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
+    else r2r_tile_body<R2R_RINV, T>(in, out, o.rp, W, Wr, Wd, idx, smem);
 }
 
 __device__ __forceinline__ int ld_acquire_gpu(const int *p) {

@@ -192,6 +192,10 @@ static int device_init() {
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT3, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_DHT, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_RFWD, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_RINV, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_RFWD, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(r2r_tile_kernel<R2R_RINV, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         if (cudaGetLastError() != cudaSuccess) g_dev_status = JT_ECUDA;
     });
     return g_dev_status;
@@ -818,6 +822,13 @@ template <typename X> static int cached(int64_t n, std::shared_ptr<X> &out) {
     return JT_OK;
 }
 
+// One-kernel line form (defined below, after the real and r2r plans)
+template <typename T> struct Real1;
+template <typename T> static bool r2r_fused_ok(const Ctx &, int64_t n, const Real1<T> *rf);
+template <typename T>
+static int r2r_fused(Ctx &ctx, int op, const Real1<T> *rf, const T *in, T *out, int64_t nlines, const Layout &lin,
+                     const Layout &lout, int dst, double mult, double mult0, const typename V2<T>::t *Wd);
+
 // ---------------------------------------------------------------------------
 // Real FFT of length n (packed layouts of fft/DoubleFFT_1D.java:433-451)
 // ---------------------------------------------------------------------------
@@ -843,11 +854,21 @@ template <typename T> struct Real1 {
         return JT_OK;
     }
     bool even() const { return n >= 2 && n % 2 == 0; }
+    bool fused_here(const Ctx &ctx) const {
+        return (sizeof(T) == 8 || ctx.rec || ctx.rec_sizing) && r2r_fused_ok<T>(ctx, n, this);
+    }
 
     // In place: n reals at a + b*dist -> packed spectrum.  dist must be even
     // for even n (the complex view).
     int fwd_packed(Ctx &ctx, T *a, int64_t dist, int64_t batch) const {
         if (n == 1 || batch <= 0) return JT_OK;
+        // one kernel (the half-length FFT with the real split on its store)
+        // for the FP64-bound double lines and inside batches; float lines keep
+        // the TMA-pipelined FFT and a separate split, which measured faster
+        if (fused_here(ctx)) {
+            const Layout l = {1, dist, 0, 1};
+            return r2r_fused<T>(ctx, R2R_RFWD, this, a, a, batch, l, l, 0, 1.0, 1.0, nullptr);
+        }
         if (even()) {
             JT_TRY(half->exec(ctx, (C2 *)a, dist / 2, (C2 *)a, dist / 2, batch, -1, 1.0));
             if (ctx.rec) {
@@ -932,6 +953,10 @@ template <typename T> struct Real1 {
                 } else LAUNCH1D(ctx, batch, scale_kernel<T>, a, dist, (int64_t)1, batch, factor);
             }
             return JT_OK;
+        }
+        if (fused_here(ctx)) {
+            const Layout l = {1, dist, 0, 1};
+            return r2r_fused<T>(ctx, R2R_RINV, this, a, a, batch, l, l, 0, factor * 2.0 / (double)n, 1.0, nullptr);
         }
         if (even()) {
             if (ctx.rec) {
@@ -1056,7 +1081,9 @@ static int r2r_fused(Ctx &ctx, int op, const Real1<T> *rf, const T *in, T *out, 
     const C2 *W = rf->half->W;
     if (op == R2R_DCT2) r2r_tile_kernel<R2R_DCT2, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
     else if (op == R2R_DCT3) r2r_tile_kernel<R2R_DCT3, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
-    else r2r_tile_kernel<R2R_DHT, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
+    else if (op == R2R_DHT) r2r_tile_kernel<R2R_DHT, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
+    else if (op == R2R_RFWD) r2r_tile_kernel<R2R_RFWD, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
+    else r2r_tile_kernel<R2R_RINV, T><<<(unsigned)grid, threads, smem, ctx.s>>>(in, out, p, W, rf->Wr, Wd);
     g_launches++;
     return JT_OK;
 }

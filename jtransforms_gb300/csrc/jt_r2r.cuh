@@ -15,10 +15,15 @@
 //                            Z_k from V_k and V_{h-k} (inverse real split)
 //                     store: x_2j = v_j, x_2j+1 = v_{n-1-j} (DST: odd
 //                            outputs negated), after the e^{+} h-point FFT
+//   realForward       load:  z_m = x_2m + i x_2m+1;  store: the packed layout
+//                            (a_0 = X_0, a_1 = X_{n/2}, a_2k + i a_2k+1 = X_k)
+//   realInverse       load:  the packed spectrum; Z_k from X_k and X_{h-k};
+//                     store: x_2m + i x_2m+1 = z_m after the e^{+} FFT
 // The arithmetic is the same as the separate pre/post kernels of
 // jt_device.cuh, which the batch recorder and odd lengths still use.
 // Reference: dct/DoubleDCT_1D.java:169-440, dst/DoubleDST_1D.java:96-328,
-// dht/DoubleDHT_1D.java:94-276.
+// dht/DoubleDHT_1D.java:94-276, fft/DoubleFFT_1D.java:524-561 (realForward,
+// rftfsub) and :946-989 (realInverse, rftbsub).
 #pragma once
 
 #include "jt_device.cuh"
@@ -28,7 +33,10 @@ namespace jt {
 
 #define C2 typename V2<T>::t
 
-enum R2rOp { R2R_DCT2 = 0, R2R_DCT3 = 1, R2R_DHT = 2 };
+enum R2rOp { R2R_DCT2 = 0, R2R_DCT3 = 1, R2R_DHT = 2, R2R_RFWD = 3, R2R_RINV = 4 };
+
+// inverse-type ops build Z from their staged input and run the e^{+} FFT
+__host__ __device__ constexpr bool r2r_inverse(int op) { return op == R2R_DCT3 || op == R2R_RINV; }
 
 struct R2rParams {
     int n;                  // real line length (even)
@@ -38,7 +46,8 @@ struct R2rParams {
     int64_t nlines;
     Layout lin, lout;       // line layouts in scalars (T units)
     int dst;                // DST: sign flips and reversal around the DCT
-    double mult, mult0;     // output (forward) or coefficient (inverse) scale; index 0 apart
+    double mult, mult0;     // output (forward) or coefficient (inverse DCT) scale, index 0 apart;
+                            // realInverse: the multiplier of Z
     float multf, mult0f;
 };
 
@@ -58,6 +67,39 @@ template <typename T> __device__ __forceinline__ C2 r2r_v(const C2 *z, int k, in
     C2 xk;
     real_split<T>(z[pad(k)], z[pad(h - k)], r2r_wr<T>(Wr, k, h), xk);
     return xk;
+}
+
+// Z_k (0 <= k < h) of the inverse ops from the staged input, a line of n
+// reals read through get(j): the (pre-scaled) DCT coefficients, whose V_k =
+// e^{+i pi k/2n}(C_k - i C_{n-k}), or the packed spectrum X (realInverse).
+// Z_k = m (0.5 (X_k + conj X_{h-k}) + 0.5 i e^{+2 pi i k/n} (X_k - conj X_{h-k})),
+// Z_0 = m (0.5 (X_0 + X_h), 0.5 (X_0 - X_h)).
+template <int OP, typename T, typename Get>
+__device__ __forceinline__ C2 r2r_inv_z(Get &get, int k, int h, const C2 *__restrict__ Wr, const C2 *__restrict__ Wd,
+                                        T m) {
+    const int n = 2 * h;
+    auto X = [&](int kk) -> C2 {
+        if (OP == R2R_DCT3) {
+            const C2 w = __ldg(&Wd[kk]);  // e^{-i pi k/2n}; conjugated below
+            const T a = kk >= n ? (T)0 : get(kk), b = kk == 0 ? (T)0 : get(n - kk);
+            return cmul<T>(mk<T>(w.x, -w.y), mk<T>(a, -b));
+        } else {
+            if (kk == 0) return mk<T>(get(0), (T)0);
+            if (kk == h) return mk<T>(get(1), (T)0);
+            return mk<T>(get(2 * kk), get(2 * kk + 1));
+        }
+    };
+    if (k == 0) {
+        const T x0 = X(0).x, xh = X(h).x;
+        return mk<T>((T)0.5 * (x0 + xh) * m, (T)0.5 * (x0 - xh) * m);
+    }
+    const C2 xk = X(k), xh = X(h - k);
+    const C2 wr = r2r_wr<T>(Wr, k, h);
+    const C2 w = mk<T>(wr.x, -wr.y);  // e^{+2 pi i k/n}
+    const C2 sa = mk<T>((T)0.5 * (xk.x + xh.x), (T)0.5 * (xk.y - xh.y));
+    const C2 d = mk<T>((T)0.5 * (xk.x - xh.x), (T)0.5 * (xk.y + xh.y));
+    const C2 wd = cmul<T>(w, d);
+    return mk<T>((sa.x - wd.y) * m, (sa.y + wd.x) * m);
 }
 
 // Tile `blk` (lines blk*C ..) run by the calling CTA, any block size, its
@@ -107,6 +149,57 @@ __device__ __forceinline__ void r2r_store(const C2 *z, int RX, T *out, const R2r
                                           int nt) {
     const int n = p.n, h = n >> 1;
     const bool rows_out = p.lout.estride == 1;
+    if (OP == R2R_RINV) {
+        const int tot = lines * n;
+        for (int idx = tid; idx < tot; idx += nt) {
+            int c, k;
+            if (rows_out) {
+                c = idx / n;
+                k = idx - c * n;
+            } else {
+                k = idx / lines;
+                c = idx - k * lines;
+            }
+            out[line_off(p.lout, b0 + c) + (int64_t)k * p.lout.estride] =
+                reinterpret_cast<const T *>(&z[c * RX + pad(k >> 1)])[k & 1];
+        }
+        return;
+    }
+    if (OP == R2R_RFWD) {
+        // packed realForward: X_kk and X_{h-kk} from the pair (the halves
+        // of a and d are exact scalings, applied at the end)
+        const int npair = h / 2 + 1;
+        const int tot = lines * npair;
+        for (int idx = tid; idx < tot; idx += nt) {
+            int c, kk;
+            if (rows_out) {
+                c = idx / npair;
+                kk = idx - c * npair;
+            } else {
+                kk = idx / lines;
+                c = idx - kk * lines;
+            }
+            T *o = out + line_off(p.lout, b0 + c);
+            const int64_t es = p.lout.estride;
+            const C2 *zl = z + c * RX;
+            if (kk == 0) {
+                const C2 z0 = zl[0];
+                o[0] = z0.x + z0.y;
+                o[es] = z0.x - z0.y;
+                continue;
+            }
+            const C2 zk = zl[pad(kk)], zh = zl[pad(h - kk)];
+            const C2 a = mk<T>(zk.x + zh.x, zk.y - zh.y), d = mk<T>(zk.x - zh.x, zk.y + zh.y);
+            const C2 wd = cmul<T>(r2r_wr<T>(Wr, kk, h), d);
+            o[(int64_t)(2 * kk) * es] = (T)0.5 * (a.x + wd.y);
+            o[(int64_t)(2 * kk + 1) * es] = (T)0.5 * (a.y - wd.x);
+            if (2 * kk != h) {
+                o[(int64_t)(2 * (h - kk)) * es] = (T)0.5 * (a.x - wd.y);
+                o[(int64_t)(2 * (h - kk) + 1) * es] = (T)0.5 * (-a.y - wd.x);
+            }
+        }
+        return;
+    }
     if (OP == R2R_DCT3) {
         const int tot = lines * n;
         for (int idx = tid; idx < tot; idx += nt) {
@@ -182,8 +275,10 @@ __device__ void r2r_tile_body(const T *in, T *out, const R2rParams &p, const C2 
             const int j = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
             if (p.dst && (i & 1)) x = -x;
             slot(bufA, c, j) = x;
-        } else if (OP == R2R_DHT) {
+        } else if (OP == R2R_DHT || OP == R2R_RFWD) {
             slot(bufA, c, i) = x;
+        } else if (OP == R2R_RINV) {
+            slot(bufB, c, i) = x;
         } else {
             // coefficient k (DST: read reversed), scaled
             const int k = p.dst ? n - 1 - i : i;
@@ -191,36 +286,18 @@ __device__ void r2r_tile_body(const T *in, T *out, const R2rParams &p, const C2 
         }
     }
     __syncthreads();
-    if (OP == R2R_DCT3) {
-        // Z_k = 0.5 (V_k + conj V_{h-k}) + 0.5 i e^{+2 pi i k/n} (V_k - conj V_{h-k})
-        auto coef = [&](int c, int k) -> T { return k >= n ? (T)0 : slot(bufB, c, k); };
-        auto vk = [&](int c, int k) -> C2 {
-            const C2 w = __ldg(&Wd[k]);  // e^{-i pi k/2n}; conjugated below
-            const T a = coef(c, k), b = k == 0 ? (T)0 : coef(c, n - k);
-            return cmul<T>(mk<T>(w.x, -w.y), mk<T>(a, -b));
-        };
+    if (r2r_inverse(OP)) {
+        const T zm = OP == R2R_RINV ? mult : (T)1;
         const int q = lines * h;
         for (int idx = threadIdx.x; idx < q; idx += blockDim.x) {
             const int c = idx / h, k = idx - c * h;
-            C2 z;
-            if (k == 0) {
-                const T x0 = vk(c, 0).x, xh = vk(c, h).x;
-                z = mk<T>((T)0.5 * (x0 + xh), (T)0.5 * (x0 - xh));
-            } else {
-                const C2 xk = vk(c, k), xh = vk(c, h - k);
-                const C2 wr = r2r_wr<T>(Wr, k, h);
-                const C2 w = mk<T>(wr.x, -wr.y);  // e^{+2 pi i k/n}
-                const C2 sa = mk<T>((T)0.5 * (xk.x + xh.x), (T)0.5 * (xk.y - xh.y));
-                const C2 d = mk<T>((T)0.5 * (xk.x - xh.x), (T)0.5 * (xk.y + xh.y));
-                const C2 wd = cmul<T>(w, d);
-                z = mk<T>(sa.x - wd.y, sa.y + wd.x);
-            }
-            bufA[c * Lp + pad(k)] = z;
+            auto get = [&](int j) -> T { return slot(bufB, c, j); };
+            bufA[c * Lp + pad(k)] = r2r_inv_z<OP, T>(get, k, h, Wr, Wd, zm);
         }
         __syncthreads();
     }
-    const C2 *z = OP == R2R_DCT3 ? tile_passes<1, T>(bufA, bufB, lines, h, Lp, p.npass, p.radix, W)
-                                 : tile_passes<-1, T>(bufA, bufB, lines, h, Lp, p.npass, p.radix, W);
+    const C2 *z = r2r_inverse(OP) ? tile_passes<1, T>(bufA, bufB, lines, h, Lp, p.npass, p.radix, W)
+                                  : tile_passes<-1, T>(bufA, bufB, lines, h, Lp, p.npass, p.radix, W);
     r2r_store<OP, T>(z, Lp, out, p, b0, lines, Wr, Wd, mult, mult0, threadIdx.x, blockDim.x);
 }
 
@@ -239,7 +316,7 @@ __global__ void __launch_bounds__(512) r2r_tile_kernel(const T *in, T *out, R2rP
 // serves as the load staging, the pass exchange and the output staging.
 // ---------------------------------------------------------------------------
 template <typename T, int H, int OP> struct R2rReg {
-    static constexpr int SIGN = OP == R2R_DCT3 ? 1 : -1;
+    static constexpr int SIGN = r2r_inverse(OP) ? 1 : -1;
     typedef Stockham<T, H, 0, SIGN> S;
     static constexpr int RX = S::LP;  // row stride of a line in the buffer (complex)
     static constexpr size_t SMEM = (size_t)S::C * RX * sizeof(typename V2<T>::t);
@@ -285,7 +362,7 @@ __global__ void __launch_bounds__(R2rReg<T, H, OP>::S::NT)
             const int j = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
             if (p.dst && (i & 1)) x = -x;
             slot(cc, j) = x;
-        } else if (OP == R2R_DHT) {
+        } else if (OP == R2R_DHT || OP == R2R_RFWD || OP == R2R_RINV) {
             slot(cc, i) = x;
         } else {
             const int k = p.dst ? n - 1 - i : i;
@@ -294,30 +371,12 @@ __global__ void __launch_bounds__(R2rReg<T, H, OP>::S::NT)
     }
     __syncthreads();
     C2 v[S::E];
-    if (OP == R2R_DCT3) {
-        // this thread's inputs Z_k, k = t + m TL, from the coefficients
-        auto coef = [&](int k) -> T { return k >= n ? (T)0 : slot(c, k); };
-        auto vk = [&](int k) -> C2 {
-            const C2 w = __ldg(&Wd[k]);
-            const T a = coef(k), b = k == 0 ? (T)0 : coef(n - k);
-            return cmul<T>(mk<T>(w.x, -w.y), mk<T>(a, -b));
-        };
+    if (r2r_inverse(OP)) {
+        // this thread's inputs Z_k, k = t + m TL, from the staged line
+        const T zm = OP == R2R_RINV ? mult : (T)1;
+        auto get = [&](int j) -> T { return slot(c, j); };
 #pragma unroll
-        for (int m = 0; m < S::E; m++) {
-            const int k = t + m * S::TL;
-            if (k == 0) {
-                const T x0 = vk(0).x, xh = vk(H).x;
-                v[m] = mk<T>((T)0.5 * (x0 + xh), (T)0.5 * (x0 - xh));
-            } else {
-                const C2 xk = vk(k), xh = vk(H - k);
-                const C2 wr = r2r_wr<T>(Wr, k, H);
-                const C2 w = mk<T>(wr.x, -wr.y);
-                const C2 sa = mk<T>((T)0.5 * (xk.x + xh.x), (T)0.5 * (xk.y - xh.y));
-                const C2 d = mk<T>((T)0.5 * (xk.x - xh.x), (T)0.5 * (xk.y + xh.y));
-                const C2 wd = cmul<T>(w, d);
-                v[m] = mk<T>(sa.x - wd.y, sa.y + wd.x);
-            }
-        }
+        for (int m = 0; m < S::E; m++) v[m] = r2r_inv_z<OP, T>(get, t + m * S::TL, H, Wr, Wd, zm);
     } else {
 #pragma unroll
         for (int m = 0; m < S::E; m++) v[m] = buf[c * RX + pad(t + m * S::TL)];
@@ -351,7 +410,9 @@ template <typename T, int H> struct R2rRegLaunch {
     static void go(int op, const T *in, T *out, const R2rParams &p, const C2 *Wp, const C2 *Wr, const C2 *Wd, cudaStream_t s) {
         if (op == R2R_DCT2) one<R2R_DCT2>(in, out, p, Wp, Wr, Wd, s);
         else if (op == R2R_DCT3) one<R2R_DCT3>(in, out, p, Wp, Wr, Wd, s);
-        else one<R2R_DHT>(in, out, p, Wp, Wr, Wd, s);
+        else if (op == R2R_DHT) one<R2R_DHT>(in, out, p, Wp, Wr, Wd, s);
+        else if (op == R2R_RFWD) one<R2R_RFWD>(in, out, p, Wp, Wr, Wd, s);
+        else one<R2R_RINV>(in, out, p, Wp, Wr, Wd, s);
     }
 };
 
