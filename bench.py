@@ -474,10 +474,31 @@ def mixed_batch(args, rng, flush, stream):
     t_pers = timed_calls([lambda: batch.run()], restore, flush, steps, warm, stream)[0]
     t_each = timed_calls([lambda: batch.run_per_transform()], restore, flush, max(2, steps // 2), 1, stream)[0]
     mg, mp, me = statistics.median(t_graph), statistics.median(t_pers), statistics.median(t_each)
+    # time per kind and size class: the same descriptors split into batches
+    # of one kind (power of two, 7-smooth, Bluestein for the FFT kinds)
+    def size_class(n):
+        if n & (n - 1) == 0:
+            return "pow2"
+        m = n
+        for p in (2, 3, 5, 7):
+            while m % p == 0:
+                m //= p
+        return "smooth" if m == 1 else "other"
+    groups = {}
+    for it, ((kind, n), _, _) in zip(items, items_spec):
+        groups.setdefault(f"{kind}_{size_class(n)}", []).append((it, (5.0 if kind == "cf" else 2.5) * n * math.log2(n)))
+    per_kind = {}
+    for name, lst in sorted(groups.items()):
+        sub = N.Batch([x[0] for x in lst])
+        tk = timed_calls([lambda: sub.run()], restore, flush, steps, warm, stream)[0]
+        mk = statistics.median(tk)
+        per_kind[name] = {"transforms": len(lst), "ms": mk, "GFLOP/s": sum(x[1] for x in lst) / (mk * 1e-3) / 1e9}
+        del sub
     return {"value": len(desc) / (mg * 1e-3), "unit": "transforms/s", "ms": mg,
             "persistent_launch_ms": mp, "per_transform_launches_ms": me,
             "speedup_vs_per_transform": me / mg, "GFLOP/s": flops / (mg * 1e-3) / 1e9,
             "distinct_plans": len(plans), "transforms": len(desc),
+            "per_kind_alone": per_kind,
             "flops": "5N log2N complex, 2.5N log2N real and DCT"}
 
 

@@ -17,10 +17,11 @@
 #include "jt_device.cuh"
 #include "jt_stockham.cuh"
 #include "jt_r2r.cuh"
+#include "jt_chirp.cuh"
 
 namespace jt {
 
-enum BOpType { BOP_TILE = 0, BOP_STOCK = 1, BOP_ELEM = 2, BOP_R2R = 3 };
+enum BOpType { BOP_TILE = 0, BOP_STOCK = 1, BOP_ELEM = 2, BOP_R2R = 3, BOP_BLUE = 4 };
 
 enum ElemKind {
     EK_COPY_COMPLEX = 0,
@@ -56,9 +57,12 @@ struct BOp {
     int ntasks;  // CTA work units
     int64_t total;  // elementwise: number of indices
     // tile / stock
-    TileParams tp;
-    StockParams sp;
-    R2rParams rp;  // DCT/DST/DHT lines in one step (kind: the R2rOp)
+    union {
+        TileParams tp;
+        StockParams sp;
+        R2rParams rp;   // DCT/DST/DHT and packed real lines in one step (kind: the R2rOp)
+        BlueParams bp;  // a Bluestein transform in one step (W, Whi, Wlo: roots, bk1, bk2)
+    };
     const void *in;
     void *out;
     const void *W, *Whi, *Wlo;
@@ -199,6 +203,14 @@ __global__ void __launch_bounds__(JT_BATCH_THREADS, 1)
                 } else {
                     if (o.sign < 0) tile_fft_body<-1, double>((const double2 *)o.in, (double2 *)o.out, o.tp, (const double2 *)o.W, (const double2 *)o.Whi, (const double2 *)o.Wlo, tk.idx, smem_raw);
                     else tile_fft_body<1, double>((const double2 *)o.in, (double2 *)o.out, o.tp, (const double2 *)o.W, (const double2 *)o.Whi, (const double2 *)o.Wlo, tk.idx, smem_raw);
+                }
+            } else if (o.type == BOP_BLUE) {
+                if (o.prec == 0) {
+                    if (o.sign < 0) blue_tile_body<-1, float>((const float2 *)o.in, (float2 *)o.out, o.bp, (const float2 *)o.W, (const float2 *)o.Whi, (const float2 *)o.Wlo, tk.idx, smem_raw);
+                    else blue_tile_body<1, float>((const float2 *)o.in, (float2 *)o.out, o.bp, (const float2 *)o.W, (const float2 *)o.Whi, (const float2 *)o.Wlo, tk.idx, smem_raw);
+                } else {
+                    if (o.sign < 0) blue_tile_body<-1, double>((const double2 *)o.in, (double2 *)o.out, o.bp, (const double2 *)o.W, (const double2 *)o.Whi, (const double2 *)o.Wlo, tk.idx, smem_raw);
+                    else blue_tile_body<1, double>((const double2 *)o.in, (double2 *)o.out, o.bp, (const double2 *)o.W, (const double2 *)o.Whi, (const double2 *)o.Wlo, tk.idx, smem_raw);
                 }
             } else if (o.type == BOP_R2R) {
                 if (o.prec == 0) r2r_dispatch<float>(o, tk.idx, smem_raw);

@@ -17,6 +17,7 @@
 #include "jt_stockham.cuh"
 #include "jt_batch.cuh"
 #include "jt_r2r.cuh"
+#include "jt_chirp.cuh"
 #include "jt_plan_table.h"
 #include "../../include/jtgpu.h"
 
@@ -192,6 +193,10 @@ static int device_init() {
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_DCT3, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_DHT, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(blue_tile_kernel<-1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(blue_tile_kernel<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(blue_tile_kernel<-1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+        cudaFuncSetAttribute(blue_tile_kernel<1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_RFWD, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_RINV, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
         cudaFuncSetAttribute(r2r_tile_kernel<R2R_RFWD, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
@@ -465,6 +470,61 @@ template <typename T> struct Fft1 {
 
     int make_chirp();
 
+    // Bluestein in one CTA tile (jt_chirp.cuh) when the padded length fits
+    // the tile passes: always inside batches, and for float calls (double
+    // calls keep the register-kernel FFTs of the FP64-bound convolution)
+    bool blue_fused_ok(const Ctx &ctx) const {
+        return pbl && pbl->algo == ALG_DIRECT && pbl->W && generic_ok(nB) && (ctx.rec || ctx.rec_sizing || sizeof(T) == 4);
+    }
+    int exec_blue_fused(Ctx &ctx, const C2 *in, int64_t din, C2 *out, int64_t dout, int64_t batch, int sign,
+                        double scale) const {
+        BlueParams p;
+        memset(&p, 0, sizeof(p));
+        p.n = (int)n;
+        p.nB = (int)nB;
+        std::vector<int> rr = direct_radices(nB);
+        if (rr.empty() || (int)rr.size() > JT_MAX_PASSES) return JT_EINVAL;
+        p.npass = (int)rr.size();
+        for (int i = 0; i < p.npass; i++) p.radix[i] = rr[i];
+        const size_t per_line = 2 * (size_t)padded_len((int)nB) * sizeof(C2);
+        int C = (int)std::max<int64_t>(1, (sizeof(T) == 4 ? 4096 : 2048) / nB);
+        C = std::min(C, (int)std::max<size_t>(1, (size_t)g_smem_optin / per_line));
+        if ((int64_t)C > batch) C = (int)batch;
+        p.C = C;
+        p.nlines = batch;
+        p.lin = Layout{1, din, 0, 1};
+        p.lout = Layout{1, dout, 0, 1};
+        p.scale = scale;
+        p.scalef = (float)scale;
+        if (ctx.rec) {
+            BOp o;
+            memset(&o, 0, sizeof(o));
+            o.type = BOP_BLUE;
+            o.prec = sizeof(T) == 4 ? 0 : 1;
+            o.sign = sign;
+            o.in = in;
+            o.out = out;
+            o.W = pbl->W;
+            o.Whi = bk1;
+            o.Wlo = bk2;
+            o.bp = p;
+            o.ntasks = (int)cdiv(batch, C);
+            o.smem = (int)(per_line * C);
+            emit(ctx, o);
+            return JT_OK;
+        }
+        if (ctx.dry) return JT_OK;  // no scratch
+        const int64_t grid = cdiv(batch, C);
+        if (grid > 0x7fffffff) return JT_ETOOBIG;
+        const int threads = (int)std::min<int64_t>(512, std::max<int64_t>(64, cdiv((int64_t)C * nB / 16, 32) * 32));
+        if (sign < 0)
+            blue_tile_kernel<-1, T><<<(unsigned)grid, threads, per_line * C, ctx.s>>>(in, out, p, pbl->W, bk1, bk2);
+        else
+            blue_tile_kernel<1, T><<<(unsigned)grid, threads, per_line * C, ctx.s>>>(in, out, p, pbl->W, bk1, bk2);
+        g_launches++;
+        return JT_OK;
+    }
+
     // Batch recording of a line pass: the generic tile kernel (any layout,
     // lengths up to the tile kernel's limit) or, for the one double
     // power-of-two length beyond it (8192), the plain register kernel.
@@ -690,6 +750,7 @@ template <typename T> struct Fft1 {
                 return JT_OK;
             }
             case ALG_BLUESTEIN: {
+                if (blue_fused_ok(ctx)) return exec_blue_fused(ctx, in, din, out, dout, batch, sign, scale);
                 int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)(128ll << 20) / (nB * (int64_t)sizeof(C2))));
                 C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * chunk * nB, ctx.dry);
                 for (int64_t b = 0; b < batch; b += chunk) {
