@@ -252,6 +252,9 @@ enum { ALG_DIRECT = 0, ALG_TWOPASS = 1, ALG_BLUESTEIN = 2, ALG_TRIVIAL = 3, ALG_
 static constexpr int64_t kPow2PassMax = (int64_t)1 << 32;
 
 static const int kMaxThreads = 512;
+// elements per task of a recorded (batch) tile step: the batch kernel's 512
+// threads then all own a radix-16 butterfly (shared memory permitting)
+static const int64_t kBatchTileElems = 16 * JT_BATCH_THREADS;
 
 template <typename T> struct Lim {
     static int64_t lmax() { return sizeof(T) == 4 ? 8192 : 4096; }
@@ -487,7 +490,7 @@ template <typename T> struct Fft1 {
         p.npass = (int)rr.size();
         for (int i = 0; i < p.npass; i++) p.radix[i] = rr[i];
         const size_t per_line = 2 * (size_t)padded_len((int)nB) * sizeof(C2);
-        int C = (int)std::max<int64_t>(1, (sizeof(T) == 4 ? 4096 : 2048) / nB);
+        int C = (int)std::max<int64_t>(1, (ctx.rec ? kBatchTileElems : (sizeof(T) == 4 ? 4096 : 2048)) / nB);
         C = std::min(C, (int)std::max<size_t>(1, (size_t)g_smem_optin / per_line));
         if ((int64_t)C > batch) C = (int)batch;
         p.C = C;
@@ -543,7 +546,7 @@ template <typename T> struct Fft1 {
             const int L = (int)n;
             const int Lp = padded_len(L);
             const bool strided = lin.estride != 1 || lout.estride != 1;
-            int64_t target = sizeof(T) == 4 ? 4096 : 2048;
+            int64_t target = kBatchTileElems;  // the batch CTA has 512 threads: 512 radix-16 butterflies
             int C = (int)std::max<int64_t>(1, target / L);
             if (strided) C = std::max(C, sizeof(T) == 4 ? 16 : 8);
             size_t per_line = 2 * (size_t)Lp * sizeof(C2);
@@ -1087,7 +1090,7 @@ static int r2r_fused(Ctx &ctx, int op, const Real1<T> *rf, const T *in, T *out, 
     for (int i = 0; i < p.npass; i++) p.radix[i] = rr[i];
     const int Lp = padded_len((int)h);
     const bool strided = lin.estride != 1 || lout.estride != 1;
-    int C = (int)std::max<int64_t>(1, (sizeof(T) == 4 ? 4096 : 2048) / h);
+    int C = (int)std::max<int64_t>(1, (ctx.rec ? kBatchTileElems : (sizeof(T) == 4 ? 4096 : 2048)) / h);
     if (strided) C = std::max(C, sizeof(T) == 4 ? 16 : 8);
     const size_t per_line = 2 * (size_t)Lp * sizeof(C2);
     C = std::min(C, (int)std::max<size_t>(1, (size_t)g_smem_optin / per_line));
