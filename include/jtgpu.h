@@ -182,6 +182,9 @@ int jt_batch_destroy(jt_batch *batch);
 #define JT_OPT_BATCH_STALL_TEST 9 /* failure-path test hook (default 0): 1 makes jt_batch_create add a step
                                      that never runs as the dependency of every transform's first step,
                                      so the waits run out and the run reports JT_ETIMEOUT */
+#define JT_OPT_TILE_ELEMS 10     /* elements per CTA of the mixed-radix tile kernel, which sets lines and
+                                     threads per CTA (default 0: the tuned table of jt_plan_table.h);
+                                     the autotuner's probe */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 

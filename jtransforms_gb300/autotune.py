@@ -17,7 +17,15 @@ into `jt_plan_table.h`, which the library compiles in (a precision that was
 not tuned keeps its current table rows). All measurements go to
 `plan_table_f32.json` / `plan_table_f64.json` beside it.
 
+With `--tile` it tunes instead the mixed-radix tile kernel: for each size
+class ceil(log2 L) and precision it times a 3 * 2^k length (a length the tile
+kernel runs) over a 256 MiB batch with each candidate number of elements per
+CTA (which sets the lines and threads per CTA), through JT_OPT_TILE_ELEMS,
+and writes the fastest into kTileElemsF32 / kTileElemsF64
+(`plan_table_tile.json`).
+
     python -m jtransforms_gb300.autotune [--prec f32|f64|both] [--lo 11] [--hi 26] [--mib 1024] [--out-dir DIR]
+    python -m jtransforms_gb300.autotune --tile [--prec f32|f64|both] [--out-dir DIR]
 """
 from __future__ import annotations
 
@@ -78,9 +86,10 @@ def time_split(N, J, torch, lg, split, mib, steps, warmup, flush, prec="f32"):
 
 
 def read_header(path: str) -> dict:
-    """The rows of the current table per precision, {prec: {lg: split}}."""
+    """The rows of the current tables: {prec: {lg: split}} for the pass
+    splits and {"tile_" + prec: {lg: elements}} for the tile kernel."""
     import re
-    out = {"f32": {}, "f64": {}}
+    out = {"f32": {}, "f64": {}, "tile_f32": {}, "tile_f64": {}}
     if not os.path.exists(path):
         return out
     text = open(path).read()
@@ -92,14 +101,23 @@ def read_header(path: str) -> dict:
         for lg, r in enumerate(rows):
             if int(r[0]) >= 0:
                 out[prec][lg] = tuple(int(v) for v in r)
+    for prec, name in (("f32", "kTileElemsF32"), ("f64", "kTileElemsF64")):
+        m = re.search(name + r"\[14\] = \{(.*?)\};", text, re.S)
+        if m:
+            for lg, v in enumerate(int(x) for x in m.group(1).split(",")):
+                if v > 0:
+                    out["tile_" + prec][lg] = v
     return out
 
 
 def write_header(best: dict, path: str):
-    """best: {prec: {lg: split}}."""
+    """best: {prec: {lg: split}, "tile_" + prec: {lg: elements}}."""
     def body(tab):
         rows = ["{%d, %d, %d}" % tuple(tab[lg]) if lg in tab else "{-1, -1, -1}" for lg in range(31)]
         return ",\n    ".join(", ".join(rows[i:i + 8]) for i in range(0, 31, 8))
+
+    def tiles(tab):
+        return ", ".join(str(tab.get(lg, 0)) for lg in range(14))
     with open(path, "w") as fh:
         fh.write("// jt_plan_table.h -- pass split per power-of-two length, indexed by log2 n:\n"
                  "// {0,0,0} one pass, {a,b,0} two passes 2^a (column) x 2^b (row), {a,b,c}\n"
@@ -108,7 +126,58 @@ def write_header(best: dict, path: str):
                  "// the measurements are in plan_table_f32.json and plan_table_f64.json.\n"
                  "#pragma once\n\n"
                  "static const signed char kSplitF32[31][3] = {\n    " + body(best["f32"]) + ",\n};\n\n"
-                 "static const signed char kSplitF64[31][3] = {\n    " + body(best["f64"]) + ",\n};\n")
+                 "static const signed char kSplitF64[31][3] = {\n    " + body(best["f64"]) + ",\n};\n\n"
+                 "// Elements per CTA of the generic tile kernel (mixed-radix lengths), indexed\n"
+                 "// by ceil(log2 L); 0: the default (4096 float, 2048 double).\n"
+                 "static const short kTileElemsF32[14] = {" + tiles(best.get("tile_f32", {})) + "};\n"
+                 "static const short kTileElemsF64[14] = {" + tiles(best.get("tile_f64", {})) + "};\n")
+
+
+def time_tile(N, J, torch, n, elems, prec, flush, steps=5, warmup=3):
+    P = N.FLOAT32 if prec == "f32" else N.FLOAT64
+    esz = 8 if prec == "f32" else 16
+    prev = N.set_option(N.OPT_TILE_ELEMS, elems)
+    try:
+        f = (J.FloatFFT_1D if prec == "f32" else J.DoubleFFT_1D)(n)
+        batch = max(1, (256 << 20) // (esz * n))
+        x = torch.randn(2 * n * batch, device="cuda", dtype=torch.float32 if prec == "f32" else torch.float64)
+        stream = torch.cuda.current_stream()
+        times = []
+        for s in range(warmup + steps):
+            flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            f.plan.execute(N.COMPLEX_FORWARD, x, 0, False, batch=batch, dist=2 * n)
+            e1.record(stream)
+            if s >= warmup:
+                times.append((e0, e1))
+        torch.cuda.synchronize()
+        ms = statistics.median(a.elapsed_time(b) for a, b in times)
+        assert f.plan.algorithm(0) == 0  # one tile pass
+        return {"ms": ms, "GB/s": 2 * esz * n * batch / (ms * 1e-3) / 1e9, "batch": batch}
+    finally:
+        N.set_option(N.OPT_TILE_ELEMS, prev)
+
+
+def tune_tiles(N, J, torch, precs, flush, out_dir):
+    best = {}
+    for prec in precs:
+        res, tab = {}, {}
+        for lg in range(4, 14 if prec == "f32" else 13):
+            n = 3 << (lg - 2)  # in (2^(lg-1), 2^lg]: ceil(log2 n) = lg
+            cand = {}
+            for elems in (512, 1024, 2048, 4096, 8192, 16384):
+                if elems < n:
+                    continue
+                cand[str(elems)] = time_tile(N, J, torch, n, elems, prec, flush)
+            key = min(cand, key=lambda k: cand[k]["ms"])
+            tab[lg] = int(key)
+            res[lg] = {"n": n, "best": int(key), "candidates": cand}
+            print(f"tile {prec} n={n}: best {key} elements per CTA, {cand[key]['GB/s']:.0f} GB/s", flush=True)
+        best["tile_" + prec] = tab
+        with open(os.path.join(out_dir, f"plan_table_tile_{prec}.json"), "w") as fh:
+            json.dump({"device": torch.cuda.get_device_name(0), "mib_per_call": 256, "sizes": res}, fh, indent=1)
+    return best
 
 
 def main(argv=None) -> int:
@@ -120,6 +189,7 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--out-dir", default="", help="where to write the header and the JSON (default: the package)")
+    ap.add_argument("--tile", action="store_true", help="tune the mixed-radix tile kernel's elements per CTA")
     args = ap.parse_args(argv)
     import torch
     sys.path.insert(0, os.path.dirname(HERE))
@@ -137,7 +207,12 @@ def main(argv=None) -> int:
     os.makedirs(out_dir, exist_ok=True)
     header = os.path.join(out_dir, "jt_plan_table.h")
     best = read_header(os.path.join(HERE, "csrc", "jt_plan_table.h"))
-    for prec in (["f32", "f64"] if args.prec == "both" else [args.prec]):
+    precs = ["f32", "f64"] if args.prec == "both" else [args.prec]
+    if args.tile:
+        best.update(tune_tiles(N, J, torch, precs, flush, args.out_dir or HERE))
+        write_header(best, header)
+        return 0
+    for prec in precs:
         results = {}
         best[prec] = {}
         for lg in range(args.lo, args.hi + 1):

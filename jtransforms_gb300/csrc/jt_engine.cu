@@ -135,6 +135,9 @@ static std::atomic<int> g_opt_direct_max_f32{8192};
 static std::atomic<int> g_opt_direct_max_f64{8192};
 static std::atomic<int> g_opt_chunk_mb{1024};
 static std::atomic<int> g_opt_host_piece_mb{64};
+// elements per CTA of the generic tile kernel (0: the tuned table, else the
+// default); the autotuner's probe
+static std::atomic<int> g_opt_tile_elems{0};
 static std::atomic<int64_t> g_opt_threepass_min{(int64_t)1 << 21};
 // pass-split overrides (jt_set_split), [precision][log2 n]; a < 0: none
 #define JT_SPLIT_MAX_LOG2 30
@@ -316,6 +319,20 @@ template <typename T> struct Fft1 {
     }
 
     static bool generic_ok(int64_t n) { return n >= 2 && n <= Lim<T>::lmax() && !direct_radices(n).empty(); }
+    // Elements per CTA of a generic tile pass over lines of length L (lines
+    // per CTA = elements / L, threads = elements / 16): the probe option, the
+    // tuned table (jt_plan_table.h, by ceil(log2 L)), or 4096 / 2048
+    static int64_t tile_elems(int L) {
+        const int o = g_opt_tile_elems.load();
+        if (o > 0) return o;
+        int lg = 0;
+        while ((1 << lg) < L) lg++;
+        if (lg < 14) {
+            const int t = sizeof(T) == 4 ? kTileElemsF32[lg] : kTileElemsF64[lg];
+            if (t > 0) return t;
+        }
+        return sizeof(T) == 4 ? 4096 : 2048;
+    }
     // register-resident power-of-two kernel (jt_stockham.cuh): row mode up to
     // reg_rows_max, column modes up to 4096
     static int64_t reg_rows_max() { return sizeof(T) == 4 ? 16384 : 8192; }
@@ -655,7 +672,7 @@ template <typename T> struct Fft1 {
         const int L = (int)n;
         const int Lp = padded_len(L);
         const bool strided = lin.estride != 1 || lout.estride != 1;
-        int64_t target = sizeof(T) == 4 ? 4096 : 2048;
+        const int64_t target = tile_elems(L);
         int C = (int)std::max<int64_t>(1, target / L);
         if (strided) C = std::max(C, sizeof(T) == 4 ? 16 : 8);
         size_t per_line = 2 * (size_t)Lp * sizeof(C2);
@@ -2135,6 +2152,10 @@ int jt_set_option(int option, int value) {
         return g_opt_batch_wait.exchange(value);
     }
     if (option == JT_OPT_BATCH_STALL_TEST) return g_opt_batch_inject.exchange(value ? 1 : 0);
+    if (option == JT_OPT_TILE_ELEMS) {
+        if (value < 0 || value > (1 << 16)) return JT_EINVAL;
+        return g_opt_tile_elems.exchange(value);
+    }
     if (option == JT_OPT_THREEPASS_MIN_LOG2) {
         if (value < 0 || value > 30) return JT_EINVAL;
         const int64_t nv = value ? (int64_t)1 << value : 0;

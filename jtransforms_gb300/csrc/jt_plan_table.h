@@ -18,3 +18,8 @@ static const signed char kSplitF64[31][3] = {
     {8, 8, 0}, {11, 6, 0}, {11, 7, 0}, {11, 8, 0}, {11, 9, 0}, {11, 10, 0}, {11, 11, 0}, {12, 11, 0},
     {8, 8, 8}, {-1, -1, -1}, {-1, -1, -1}, {-1, -1, -1}, {-1, -1, -1}, {-1, -1, -1}, {-1, -1, -1},
 };
+
+// Elements per CTA of the generic tile kernel (mixed-radix lengths), indexed
+// by ceil(log2 L); 0: the default (4096 float, 2048 double).
+static const short kTileElemsF32[14] = {0, 0, 0, 0, 512, 512, 512, 1024, 1024, 1024, 1024, 2048, 4096, 8192};
+static const short kTileElemsF64[14] = {0, 0, 0, 0, 512, 512, 512, 512, 1024, 2048, 2048, 2048, 4096, 0};
