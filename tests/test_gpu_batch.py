@@ -21,6 +21,13 @@ ITEMS = [
     ("dct", "f64", "inv", True, [128, 360, 8192]),
     ("dst", "f64", "fwd", True, [64, 300]),
     ("dht", "f32", "fwd", False, [128, 1000]),
+    # one-step forms: packed real inverse, DHT, DST inverse and DCT of even
+    # lengths whose half length is mixed-radix, Bluestein inverses
+    ("fft", "f32", "ri", True, [128, 2048, 210, 97]),
+    ("dht", "f64", "fwd", False, [64, 210, 101]),
+    ("dst", "f32", "inv", True, [32, 210, 4096]),
+    ("fft", "f64", "ci", True, [97, 1021]),
+    ("dct", "f32", "fwd", True, [210, 1024, 7]),
 ]
 
 
