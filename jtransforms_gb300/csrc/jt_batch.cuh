@@ -21,7 +21,7 @@
 
 namespace jt {
 
-enum BOpType { BOP_TILE = 0, BOP_STOCK = 1, BOP_ELEM = 2, BOP_R2R = 3, BOP_BLUE = 4 };
+enum BOpType { BOP_TILE = 0, BOP_ELEM = 2, BOP_R2R = 3, BOP_BLUE = 4 };
 
 enum ElemKind {
     EK_COPY_COMPLEX = 0,
@@ -59,7 +59,6 @@ struct BOp {
     // tile / stock
     union {
         TileParams tp;
-        StockParams sp;
         R2rParams rp;   // DCT/DST/DHT and packed real lines in one step (kind: the R2rOp)
         BlueParams bp;  // a Bluestein transform in one step (W, Whi, Wlo: roots, bk1, bk2)
     };
@@ -76,8 +75,13 @@ struct BTask {
     int idx;
 };
 
-#define JT_BATCH_THREADS 512
+// A batch CTA has 256 threads and at most JT_BATCH_SMEM_CAP bytes of shared
+// memory per task, so that two CTAs share an SM and one's loads overlap the
+// other's arithmetic (lines whose tile would need more are recorded as two
+// passes of shorter lines).
+#define JT_BATCH_THREADS 256
 #define JT_BATCH_ELEMS_PER_TASK (JT_BATCH_THREADS * 4)
+#define JT_BATCH_SMEM_CAP (110 * 1024)
 
 template <typename T> __device__ void elem_dispatch(const BOp &o, int64_t idx) {
     typedef typename V2<T>::t C2;
@@ -164,7 +168,7 @@ __device__ __forceinline__ int ld_acquire_gpu(const int *p) {
 
 // wait_polls: polls of a dependency wait (64 ns apart) before it gives up;
 // the library's default, 2^24, is about a second
-__global__ void __launch_bounds__(JT_BATCH_THREADS, 1)
+__global__ void __launch_bounds__(JT_BATCH_THREADS, 2)
     batch_kernel(const BOp *__restrict__ ops, const BTask *__restrict__ tasks, int ntasks, int *head, int *done, int *err,
                  int wait_polls) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -215,10 +219,6 @@ __global__ void __launch_bounds__(JT_BATCH_THREADS, 1)
             } else if (o.type == BOP_R2R) {
                 if (o.prec == 0) r2r_dispatch<float>(o, tk.idx, smem_raw);
                 else r2r_dispatch<double>(o, tk.idx, smem_raw);
-            } else if (o.type == BOP_STOCK) {
-                // one power-of-two double line of 8192 (too long for the tile kernel)
-                if (o.sign < 0) stockham_body<double, 8192, 0, -1>((const double2 *)o.in, (double2 *)o.out, o.sp, (const double2 *)o.W, nullptr, nullptr, tk.idx, smem_raw);
-                else stockham_body<double, 8192, 0, 1>((const double2 *)o.in, (double2 *)o.out, o.sp, (const double2 *)o.W, nullptr, nullptr, tk.idx, smem_raw);
             } else {
                 const int64_t base = (int64_t)tk.idx * JT_BATCH_ELEMS_PER_TASK;
                 for (int k = tid; k < JT_BATCH_ELEMS_PER_TASK; k += JT_BATCH_THREADS) {

@@ -255,9 +255,13 @@ enum { ALG_DIRECT = 0, ALG_TWOPASS = 1, ALG_BLUESTEIN = 2, ALG_TRIVIAL = 3, ALG_
 static constexpr int64_t kPow2PassMax = (int64_t)1 << 32;
 
 static const int kMaxThreads = 512;
-// elements per task of a recorded (batch) tile step: the batch kernel's 512
+// elements per task of a recorded (batch) tile step: the batch kernel's
 // threads then all own a radix-16 butterfly (shared memory permitting)
 static const int64_t kBatchTileElems = 16 * JT_BATCH_THREADS;
+// whether one line of length L fits a batch task's shared-memory cap
+template <typename T> static bool batch_line_ok(int64_t L) {
+    return 2 * (size_t)padded_len((int)L) * sizeof(typename V2<T>::t) <= (size_t)JT_BATCH_SMEM_CAP;
+}
 
 template <typename T> struct Lim {
     static int64_t lmax() { return sizeof(T) == 4 ? 8192 : 4096; }
@@ -434,14 +438,6 @@ template <typename T> struct Fft1 {
             f->algo = ALG_TRIVIAL;
         } else if (sp && sp[0] == 0 && reg_ok(n)) {
             JT_TRY(f->init_direct());
-            if (!generic_ok(n) && !(sizeof(T) == 8 && n == 8192)) {
-                int lg = 0;
-                while (((int64_t)1 << lg) < n) lg++;
-                f->rec_alt.reset(new (std::nothrow) Fft1());
-                if (!f->rec_alt) return JT_ENOMEM;
-                f->rec_alt->n = n;
-                JT_TRY(f->rec_alt->init_twopass((int64_t)1 << (lg / 2)));
-            }
         } else if (sp && sp[0] > 0 && sp[2] == 0 && sp[0] <= 12 && sp[1] <= 12) {
             JT_TRY(f->init_twopass((int64_t)1 << sp[0]));
         } else if (sp && sp[2] > 0 && n <= kPow2PassMax && sp[0] <= 12 && sp[1] <= 12 && sp[2] <= 12) {
@@ -484,17 +480,45 @@ template <typename T> struct Fft1 {
                 JT_TRY(f->make_chirp());
             }
         }
+        if (top) JT_TRY(f->make_rec_alt());
         out = std::move(f);
         return JT_OK;
     }
 
     int make_chirp();
 
+    // A one-pass length whose line does not fit a batch task (the tile
+    // kernel's limit or the batch's shared-memory cap) is recorded as the
+    // same transform in two passes of shorter lines: the balanced split with
+    // both lengths fitting, if there is one.
+    int make_rec_alt() {
+        if (algo != ALG_DIRECT || (generic_ok(n) && batch_line_ok<T>(n))) return JT_OK;
+        int64_t best = 0;
+        double bestd = 1e300;
+        for (int64_t d = 2; d < n && d <= Lim<T>::lmax(); d++) {
+            if (n % d) continue;
+            const int64_t e = n / d;
+            if (!generic_ok(d) || !generic_ok(e) || !batch_line_ok<T>(d) || !batch_line_ok<T>(e)) continue;
+            const double dd = std::fabs(std::log((double)d) - std::log((double)e));
+            if (dd < bestd) {
+                bestd = dd;
+                best = d;
+            }
+        }
+        if (!best) return JT_OK;
+        rec_alt.reset(new (std::nothrow) Fft1());
+        if (!rec_alt) return JT_ENOMEM;
+        rec_alt->n = n;
+        return rec_alt->init_twopass(best);
+    }
+
     // Bluestein in one CTA tile (jt_chirp.cuh) when the padded length fits
     // the tile passes: always inside batches, and for float calls (double
     // calls keep the register-kernel FFTs of the FP64-bound convolution)
     bool blue_fused_ok(const Ctx &ctx) const {
-        return pbl && pbl->algo == ALG_DIRECT && pbl->W && generic_ok(nB) && (ctx.rec || ctx.rec_sizing || sizeof(T) == 4);
+        const bool rec = ctx.rec || ctx.rec_sizing;
+        return pbl && pbl->algo == ALG_DIRECT && pbl->W && generic_ok(nB) && (rec || sizeof(T) == 4) &&
+               (!rec || batch_line_ok<T>(nB));
     }
     int exec_blue_fused(Ctx &ctx, const C2 *in, int64_t din, C2 *out, int64_t dout, int64_t batch, int sign,
                         double scale) const {
@@ -546,8 +570,8 @@ template <typename T> struct Fft1 {
     }
 
     // Batch recording of a line pass: the generic tile kernel (any layout,
-    // lengths up to the tile kernel's limit) or, for the one double
-    // power-of-two length beyond it (8192), the plain register kernel.
+    // lengths up to the tile kernel's limit; longer one-pass lengths are
+    // recorded through their two-pass alternate, make_rec_alt).
     int record_lines(Ctx &ctx, const C2 *in, C2 *out, int64_t nlines, const Layout &lin, const Layout &lout, int sign,
                      double scale, int64_t tw_n, int64_t tw_inner, const C2 *Whi_, const C2 *Wlo_, int tw_lo_bits) const {
         BOp o;
@@ -567,7 +591,7 @@ template <typename T> struct Fft1 {
             int C = (int)std::max<int64_t>(1, target / L);
             if (strided) C = std::max(C, sizeof(T) == 4 ? 16 : 8);
             size_t per_line = 2 * (size_t)Lp * sizeof(C2);
-            int cmax = (int)std::max<size_t>(1, (size_t)g_smem_optin / per_line);
+            int cmax = (int)std::max<size_t>(1, std::min<size_t>(g_smem_optin, JT_BATCH_SMEM_CAP) / per_line);
             C = std::min(C, cmax);
             if ((int64_t)C > nlines) C = (int)nlines;
             std::vector<int> rr = radix.empty() ? direct_radices(n) : radix;
@@ -587,18 +611,6 @@ template <typename T> struct Fft1 {
             o.tp.tw_lo_bits = tw_lo_bits;
             o.ntasks = (int)cdiv(nlines, C);
             o.smem = (int)(per_line * C);
-        } else if (sizeof(T) == 8 && n == 8192 && lin.estride == 1 && lout.estride == 1 && tw_n == 0) {
-            if (!Wp) return JT_EINVAL;
-            o.type = BOP_STOCK;
-            o.W = Wp;  // the register kernel reads the pass table
-            o.sp.nlines = nlines;
-            o.sp.lin = lin;
-            o.sp.lout = lout;
-            o.sp.scale = scale;
-            o.sp.scalef = (float)scale;
-            o.sp.do_scale = scale != 1.0;
-            o.ntasks = (int)nlines;
-            o.smem = (int)Stockham<double, 8192, 0, -1>::SMEM;
         } else {
             return JT_EINVAL;  // no single-CTA step for this line in a batch
         }
@@ -1069,9 +1081,9 @@ template <typename T> struct Real1 {
 // tile passes run (h = n/2 up to the tile kernel's limit, prime factors <= 63),
 // any line layout.  Batch recordings keep the separate pre/post steps.
 // ---------------------------------------------------------------------------
-template <typename T> static bool r2r_fused_ok(const Ctx &, int64_t n, const Real1<T> *rf) {
+template <typename T> static bool r2r_fused_ok(const Ctx &ctx, int64_t n, const Real1<T> *rf) {
     return n >= 4 && n % 2 == 0 && rf && rf->half && rf->half->algo == ALG_DIRECT && rf->half->W && rf->Wr &&
-           Fft1<T>::generic_ok(n / 2);
+           Fft1<T>::generic_ok(n / 2) && (!(ctx.rec || ctx.rec_sizing) || batch_line_ok<T>(n / 2));
 }
 
 // Lines per CTA of the register form for half length h (0: none): power-of-
