@@ -63,6 +63,18 @@ static int64_t next_pow2(int64_t x) {
     while (p < x) p <<= 1;
     return p;
 }
+// smallest 2^a 3^b 5^c 7^d >= x
+static int64_t next_smooth(int64_t x) {
+    int64_t best = next_pow2(x);
+    for (int64_t p7 = 1; p7 < best; p7 *= 7)
+        for (int64_t p5 = p7; p5 < best; p5 *= 5)
+            for (int64_t p3 = p5; p3 < best; p3 *= 3) {
+                int64_t v = p3;
+                while (v < x) v *= 2;
+                if (v < best) best = v;
+            }
+    return best;
+}
 
 // Per-thread device workspace: a bump allocator that is sized by a dry run
 // of the same call (no launches), then handed out in 256-byte aligned slices.
@@ -491,7 +503,23 @@ template <typename T> struct Fft1 {
     // kernel's limit or the batch's shared-memory cap) is recorded as the
     // same transform in two passes of shorter lines: the balanced split with
     // both lengths fitting, if there is one.
+    // A Bluestein length records its convolution at the smallest 7-smooth
+    // length >= 2n - 1 instead of the power of two: batch steps run every
+    // line on the mixed-radix tile passes, so the shorter convolution is
+    // less work there (up to 2x); single calls keep the power of two, whose
+    // register-kernel passes are faster.  Only for convolutions up to 2^20.
     int make_rec_alt() {
+        if (algo == ALG_BLUESTEIN) {
+            const int64_t nS = next_smooth(2 * n - 1);
+            if (nB > ((int64_t)1 << 20) || nS >= nB) return JT_OK;
+            rec_alt.reset(new (std::nothrow) Fft1());
+            if (!rec_alt) return JT_ENOMEM;
+            rec_alt->n = n;
+            rec_alt->algo = ALG_BLUESTEIN;
+            rec_alt->nB = nS;
+            JT_TRY(create(nS, rec_alt->pbl));
+            return rec_alt->make_chirp();
+        }
         if (algo != ALG_DIRECT || (generic_ok(n) && batch_line_ok<T>(n))) return JT_OK;
         int64_t best = 0;
         double bestd = 1e300;
@@ -782,6 +810,7 @@ template <typename T> struct Fft1 {
                 return JT_OK;
             }
             case ALG_BLUESTEIN: {
+                if ((ctx.rec || ctx.rec_sizing) && rec_alt) return rec_alt->exec(ctx, in, din, out, dout, batch, sign, scale);
                 if (blue_fused_ok(ctx)) return exec_blue_fused(ctx, in, din, out, dout, batch, sign, scale);
                 int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)(128ll << 20) / (nB * (int64_t)sizeof(C2))));
                 C2 *tmp = (C2 *)ctx.ws->get(sizeof(C2) * chunk * nB, ctx.dry);
