@@ -335,16 +335,25 @@ def other_workloads(args, peak, flush, stream):
             entry["binding"] = prec if cpeak < hbm_lim else "hbm"
             entry["frac_of_attainable"] = gf / min(hbm_lim, cpeak)
 
-    def measure(name, plan, op, buf, batch, dist, scale, flops, bytes_alg, unit_note, extra_fn=None):
+    def errors(entry, got, want):
+        # relative L2 and max error (max |got - want| / max |want|) of the
+        # last timed call's output against an FP64 reference
+        g64 = np.asarray(got, dtype=np.float64).ravel()
+        w64 = np.asarray(want, dtype=np.float64).ravel()
+        d = g64 - w64
+        entry["rel_l2_vs_fp64"] = float(np.linalg.norm(d) / np.linalg.norm(w64))
+        entry["rel_max_err_vs_fp64"] = float(np.abs(d).max() / np.abs(w64).max())
+
+    def measure(name, plan, op, buf, batch, dist, scale, flops, bytes_alg, unit_note, ref_fn=None):
         pristine = buf.clone()
         fns = [lambda: plan.execute(op, buf, 0, scale, batch=batch, dist=dist)]
-        if extra_fn:
-            fns = [extra_fn]
         t = timed_calls(fns, lambda i: buf.copy_(pristine), flush, steps, warm, stream)[0]
         ms = statistics.median(t)
         out[name] = {"value": flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms": ms, "best_ms": min(t),
                      "flops": unit_note}
         bound(out[name], flops, bytes_alg, ms, "fp64" if buf.dtype == torch.float64 else "fp32")
+        if ref_fn is not None:  # buf holds the last timed call's output
+            errors(out[name], buf.cpu().numpy(), ref_fn(pristine.cpu().numpy()))
 
     # config 1: 256 x DoubleFFT_1D(4096) complexForward then complexInverse(scale=true)
     n, B = 4096, 256
@@ -361,38 +370,73 @@ def other_workloads(args, peak, flush, stream):
         "value": 2 * flops_c2c(n, B) / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms": ms,
         "flops": "5N log2N x2 directions"}
     bound(out["c1_DoubleFFT_1D_4096x256_fwd_inv"], 2 * flops_c2c(n, B), 4 * 16 * n * B, ms, "fp64")
+    # the forward half against torch's complex128 FFT of the same arrays
+    y = pristine.clone()
+    f1.plan.execute(N.COMPLEX_FORWARD, y, 0, False, batch=B, dist=2 * n)
+    z = torch.fft.fft(torch.view_as_complex(pristine.view(B, n, 2)), dim=1)
+    errors(out["c1_DoubleFFT_1D_4096x256_fwd_inv"], y.cpu().numpy(), torch.view_as_real(z).cpu().numpy())
 
     # config 2a: FloatFFT_2D(2048, 2048).realForward on a blob image
     img = blob_image(2048, rng).astype(np.float32).ravel()
     f2 = J.FloatFFT_2D(2048, 2048)
     buf = torch.from_numpy(img).cuda()
     N2 = 2048 * 2048
+    def packed2d(a, R=2048, C=2048):
+        # numpy's FP64 spectrum in realForward's packed 2D layout
+        # (fft/DoubleFFT_2D.java:788-815)
+        F = np.fft.rfft2(a.astype(np.float64).reshape(R, C))
+        P = np.empty((R, C))
+        P[:, 2::2] = F[:, 1:C // 2].real
+        P[:, 3::2] = F[:, 1:C // 2].imag
+        k = np.arange(1, R // 2)
+        P[k, 0] = F[k, 0].real
+        P[k, 1] = F[k, 0].imag
+        P[R - k, 1] = F[k, C // 2].real
+        P[R - k, 0] = -F[k, C // 2].imag
+        P[0, 0], P[0, 1] = F[0, 0].real, F[0, C // 2].real
+        P[R // 2, 0], P[R // 2, 1] = F[R // 2, 0].real, F[R // 2, C // 2].real
+        return P
     measure("c2a_FloatFFT_2D_2048_realForward", f2.plan, N.REAL_FORWARD, buf, 1, N2, False,
-            2.5 * N2 * math.log2(N2), 2 * 4 * N2, "2.5N log2N")
+            2.5 * N2 * math.log2(N2), 2 * 4 * N2, "2.5N log2N", ref_fn=packed2d)
     # config 2b: DoubleDCT_2D(1024, 1024).forward(scale=true)
     img = blob_image(1024, rng).ravel()
     d2 = J.DoubleDCT_2D(1024, 1024)
     buf = torch.from_numpy(img).cuda()
     N2 = 1024 * 1024
+    import scipy.fft as sfft
     measure("c2b_DoubleDCT_2D_1024_forward", d2.plan, N.FORWARD, buf, 1, N2, True,
-            2.5 * N2 * math.log2(N2), 2 * 8 * N2, "2.5N log2N")
+            2.5 * N2 * math.log2(N2), 2 * 8 * N2, "2.5N log2N",
+            ref_fn=lambda a: sfft.dctn(a.reshape(1024, 1024), type=2, norm="ortho"))
     # config 3a: DoubleFFT_3D(256^3).complexForward, N(0,1)
     f3 = J.DoubleFFT_3D(256, 256, 256)
     N3 = 256 ** 3
     g = torch.Generator(device="cuda").manual_seed(SEED)
     buf = torch.randn(2 * N3, dtype=torch.float64, device="cuda", generator=g)
+    def fft3(a):
+        z = np.fft.fftn((a[0::2] + 1j * a[1::2]).reshape(256, 256, 256))
+        r = np.empty(2 * N3)
+        r[0::2] = z.real.ravel()
+        r[1::2] = z.imag.ravel()
+        return r
     measure("c3a_DoubleFFT_3D_256_complexForward", f3.plan, N.COMPLEX_FORWARD, buf, 1, 2 * N3, False,
-            flops_c2c(N3, 1), 2 * 16 * N3, "5N log2N")
+            flops_c2c(N3, 1), 2 * 16 * N3, "5N log2N", ref_fn=fft3)
     del buf
     # config 3b/3c: DoubleDST_3D / DoubleDHT_3D (128^3) uniform[-1, 1)
     N3 = 128 ** 3
     x = torch.from_numpy(rng.uniform(-1, 1, N3)).cuda()
     s3 = J.DoubleDST_3D(128, 128, 128)
+    x0 = x.clone()
     measure("c3b_DoubleDST_3D_128_forward", s3.plan, N.FORWARD, x, 1, N3, True,
-            2.5 * N3 * math.log2(N3), 2 * 8 * N3, "2.5N log2N")
+            2.5 * N3 * math.log2(N3), 2 * 8 * N3, "2.5N log2N",
+            ref_fn=lambda a: sfft.dstn(a.reshape(128, 128, 128), type=2, norm="ortho"))
     h3 = J.DoubleDHT_3D(128, 128, 128)
+    x.copy_(x0)
+
+    def dht3(a):
+        z = np.fft.fftn(a.reshape(128, 128, 128))
+        return z.real - z.imag
     measure("c3c_DoubleDHT_3D_128_forward", h3.plan, N.FORWARD, x, 1, N3, False,
-            2.5 * N3 * math.log2(N3), 2 * 8 * N3, "2.5N log2N")
+            2.5 * N3 * math.log2(N3), 2 * 8 * N3, "2.5N log2N", ref_fn=dht3)
     del x
     out["c5_mixed_batch_10000"] = mixed_batch(args, rng, flush, stream)
     return out
