@@ -474,7 +474,9 @@ def batch_descriptors(count, rng):
     return out
 
 
-def mixed_batch(args, rng, flush, stream):
+def mixed_batch_items(rng):
+    """The 10,000 mixed descriptors as batch items over two device buffers:
+    (items, items_spec, plans, (b32, b64), flops, desc)."""
     import torch
     from jtransforms_gb300 import _native as N
     desc = batch_descriptors(10000, rng)
@@ -498,7 +500,6 @@ def mixed_batch(args, rng, flush, stream):
     g = torch.Generator(device="cuda").manual_seed(SEED)
     b32 = torch.rand(max(f32_off, 1), dtype=torch.float32, device="cuda", generator=g) * 2 - 1
     b64 = torch.rand(max(f64_off, 1), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
-    p32, p64 = b32.clone(), b64.clone()
     opc = {"cf": N.COMPLEX_FORWARD, "rf": N.REAL_FORWARD, "dct": N.FORWARD}
     items = []
     flops = 0.0
@@ -507,6 +508,14 @@ def mixed_batch(args, rng, flush, stream):
         ptr = buf.data_ptr() + off * buf.element_size()
         items.append((plans[(kind, n)], opc[kind], ptr, kind == "dct"))
         flops += (5.0 if kind == "cf" else 2.5) * n * math.log2(n)
+    return items, items_spec, plans, (b32, b64), flops, desc
+
+
+def mixed_batch(args, rng, flush, stream):
+    import torch
+    from jtransforms_gb300 import _native as N
+    items, items_spec, plans, (b32, b64), flops, desc = mixed_batch_items(rng)
+    p32, p64 = b32.clone(), b64.clone()
     batch = N.Batch(items)
 
     def restore(i):
@@ -754,6 +763,10 @@ def profile_case(case: str) -> int:
         plan = J.DoubleDST_3D(128, 128, 128).plan
         x = torch.from_numpy(rng.uniform(-1, 1, 128 ** 3)).cuda()
         run = lambda: plan.execute(N.FORWARD, x, 0, True)  # noqa: E731
+    elif case == "batch":  # the 10,000 mixed transforms, one persistent launch per call
+        items_batch = mixed_batch_items(rng)
+        bt = N.Batch(items_batch[0])
+        run = lambda: bt.run()  # noqa: E731
     else:  # tc1024: the split tensor-core mode, 2^10 x 2^15 (256 MiB)
         n, B = 1024, 1 << 15
         plan = J.FloatFFT_1D(n).plan
@@ -788,7 +801,7 @@ def main():
     ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 1024)")
     ap.add_argument("--host-piece-mb", type=int, default=0, help="MiB per piece of the end-to-end host batch (library default 64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
-    ap.add_argument("--case", default="", choices=["", "c1", "c2b", "c3b", "tc1024"],
+    ap.add_argument("--case", default="", choices=["", "c1", "c2b", "c3b", "tc1024", "batch"],
                     help="profiling case: run one small workload a few times and exit (no JSON line)")
     args = ap.parse_args()
     global ELEMS, SIZES
