@@ -745,16 +745,34 @@ def run_ours(args, world, rank, local):
 
 def profile_case(case: str) -> int:
     """A small workload for ncu captures: three calls of one transform, then
-    (c1) the CUDA-core FMA peaks.  Prints what it ran."""
+    (c1) the CUDA-core FMA peaks.  Prints what it ran.  Case `peaks` prints
+    the measured FMA and distributed-shared-memory peaks only."""
     import torch
     import jtransforms_gb300 as J
     from jtransforms_gb300 import _native as N
     rng = np.random.default_rng(SEED)
+    if case == "peaks":  # measured FMA and distributed-shared-memory peaks, no transform
+        lib = N.load()
+        for p, name in ((N.FLOAT64, "fp64"), (N.FLOAT32, "fp32")):
+            v = ctypes.c_double()
+            rc = lib.jt_fma_peak(p, ctypes.byref(v))
+            print(f"fma peak {name}: rc {rc}, {v.value:.1f} GFLOP/s")
+        for cl in (2, 4, 8, 16):
+            for remote in (0, 1):
+                v, ctas = ctypes.c_double(), ctypes.c_int()
+                rc = lib.jt_dsmem_peak(cl, remote, ctypes.byref(v), ctypes.byref(ctas))
+                print(f"dsmem cluster {cl:2d} {'remote' if remote else 'local '}: rc {rc}, "
+                      f"{v.value:.1f} GB/s over {ctas.value} CTAs")
+        return 0
     if case == "c1":
         n, B = 4096, 256
         plan = J.DoubleFFT_1D(n).plan
         x = torch.from_numpy(rng.uniform(-1, 1, 2 * n * B)).cuda()
         run = lambda: plan.execute(N.COMPLEX_FORWARD, x, 0, False, batch=B, dist=2 * n)  # noqa: E731
+    elif case == "c2a":
+        plan = J.FloatFFT_2D(2048, 2048).plan
+        x = torch.from_numpy(blob_image(2048, rng).astype(np.float32).ravel()).cuda()
+        run = lambda: plan.execute(N.REAL_FORWARD, x, 0, False)  # noqa: E731
     elif case == "c2b":
         plan = J.DoubleDCT_2D(1024, 1024).plan
         x = torch.from_numpy(blob_image(1024, rng).ravel()).cuda()
@@ -801,7 +819,7 @@ def main():
     ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 1024)")
     ap.add_argument("--host-piece-mb", type=int, default=0, help="MiB per piece of the end-to-end host batch (library default 64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
-    ap.add_argument("--case", default="", choices=["", "c1", "c2b", "c3b", "tc1024", "batch"],
+    ap.add_argument("--case", default="", choices=["", "c1", "c2a", "c2b", "c3b", "tc1024", "batch", "peaks"],
                     help="profiling case: run one small workload a few times and exit (no JSON line)")
     args = ap.parse_args()
     global ELEMS, SIZES

@@ -207,6 +207,14 @@ int jt_plan_algorithm(const jt_plan *plan, int axis);
  * two flops) for `prec`: the compute roofline of the Double (FP64) and Float
  * paths.  No counterpart in the reference. */
 int jt_fma_peak(int prec, double *gflops);
+/* Measured aggregate read bandwidth in GB/s of shared memory within thread-block
+ * clusters of `cluster` CTAs (2, 4, 8 or 16; 128 KiB and 1024 threads per CTA,
+ * as many clusters as fit at once): remote = 1 reads peers' shared memory
+ * (distributed shared memory), remote = 0 the CTA's own.  `active_ctas`
+ * (may be NULL) receives the number of CTAs resident in that launch.  The
+ * bound of a plan that exchanges one transform between the CTAs of a
+ * cluster.  No counterpart in the reference. */
+int jt_dsmem_peak(int cluster, int remote, double *gbs, int *active_ctas);
 
 #ifdef __cplusplus
 }

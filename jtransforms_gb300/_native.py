@@ -51,6 +51,7 @@ SIGNATURES = {
     "jt_set_option": (_I, [_I, _I]),
     "jt_execute_device_noalloc": (_I, [_P, _I, _P, _P, _L, _I, _P]),
     "jt_fma_peak": (_I, [_I, ctypes.POINTER(ctypes.c_double)]),
+    "jt_dsmem_peak": (_I, [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
 }
 OPT_TMA_PIPELINE, OPT_DIRECT_MAX_F32, OPT_DIRECT_MAX_F64, OPT_COLUMN_KERNEL, OPT_TWOPASS_CHUNK_MB = 0, 1, 2, 3, 4
 OPT_THREEPASS_MIN_LOG2, OPT_HOST_PIECE_MB = 5, 6
