@@ -832,6 +832,9 @@ def main():
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup(args)
     if args.case:
+        if args.no_tma:
+            from jtransforms_gb300 import _native as N
+            N.set_option(N.OPT_TMA_PIPELINE, 0)
         return profile_case(args.case)
     if args.impl == "reference":
         return run_reference(args, world, rank)

@@ -185,6 +185,9 @@ int jt_batch_destroy(jt_batch *batch);
 #define JT_OPT_TILE_ELEMS 10     /* elements per CTA of the mixed-radix tile kernel, which sets lines and
                                      threads per CTA (default 0: the tuned table of jt_plan_table.h);
                                      the autotuner's probe */
+#define JT_OPT_REAL_FUSED_F32 11 /* 1 (default): Float packed realForward/realInverse lines with a
+                                     power-of-two half length of 16..4096 run as one kernel (FFT and
+                                     real split together); 0: the pipelined FFT and a separate split */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 

@@ -150,6 +150,7 @@ static std::atomic<int> g_opt_host_piece_mb{64};
 // elements per CTA of the generic tile kernel (0: the tuned table, else the
 // default); the autotuner's probe
 static std::atomic<int> g_opt_tile_elems{0};
+static std::atomic<int> g_opt_real_fused_f32{1};
 static std::atomic<int64_t> g_opt_threepass_min{(int64_t)1 << 21};
 // pass-split overrides (jt_set_split), [precision][log2 n]; a < 0: none
 #define JT_SPLIT_MAX_LOG2 30
@@ -947,6 +948,7 @@ template <typename X> static int cached(int64_t n, std::shared_ptr<X> &out) {
 // One-kernel line form (defined below, after the real and r2r plans)
 template <typename T> struct Real1;
 template <typename T> static bool r2r_fused_ok(const Ctx &, int64_t n, const Real1<T> *rf);
+template <typename T> static int r2r_reg_c(int64_t h, const Real1<T> *rf);
 template <typename T>
 static int r2r_fused(Ctx &ctx, int op, const Real1<T> *rf, const T *in, T *out, int64_t nlines, const Layout &lin,
                      const Layout &lout, int dst, double mult, double mult0, const typename V2<T>::t *Wd);
@@ -976,8 +978,14 @@ template <typename T> struct Real1 {
         return JT_OK;
     }
     bool even() const { return n >= 2 && n % 2 == 0; }
-    bool fused_here(const Ctx &ctx) const {
-        return (sizeof(T) == 8 || ctx.rec || ctx.rec_sizing) && r2r_fused_ok<T>(ctx, n, this);
+    // One kernel for packed realForward/realInverse: the FP64-bound double
+    // lines, batch steps, and float lines with a register form whose scalar
+    // pairs are aligned complex values (paired loads and stores)
+    bool fused_here(const Ctx &ctx, const T *a, int64_t dist) const {
+        if (!r2r_fused_ok<T>(ctx, n, this)) return false;
+        if (sizeof(T) == 8 || ctx.rec || ctx.rec_sizing) return true;
+        return g_opt_real_fused_f32.load() != 0 && r2r_reg_c<T>(n / 2, this) > 0 && dist % 2 == 0 &&
+               ((uintptr_t)a % sizeof(C2)) == 0;
     }
 
     // In place: n reals at a + b*dist -> packed spectrum.  dist must be even
@@ -985,9 +993,9 @@ template <typename T> struct Real1 {
     int fwd_packed(Ctx &ctx, T *a, int64_t dist, int64_t batch) const {
         if (n == 1 || batch <= 0) return JT_OK;
         // one kernel (the half-length FFT with the real split on its store)
-        // for the FP64-bound double lines and inside batches; float lines keep
-        // the TMA-pipelined FFT and a separate split, which measured faster
-        if (fused_here(ctx)) {
+        // where fused_here allows; otherwise the TMA-pipelined FFT and a
+        // separate split
+        if (fused_here(ctx, a, dist)) {
             const Layout l = {1, dist, 0, 1};
             return r2r_fused<T>(ctx, R2R_RFWD, this, a, a, batch, l, l, 0, 1.0, 1.0, nullptr);
         }
@@ -1076,7 +1084,7 @@ template <typename T> struct Real1 {
             }
             return JT_OK;
         }
-        if (fused_here(ctx)) {
+        if (fused_here(ctx, a, dist)) {
             const Layout l = {1, dist, 0, 1};
             return r2r_fused<T>(ctx, R2R_RINV, this, a, a, batch, l, l, 0, factor * 2.0 / (double)n, 1.0, nullptr);
         }
@@ -1162,6 +1170,13 @@ static int r2r_fused(Ctx &ctx, int op, const Real1<T> *rf, const T *in, T *out, 
     p.mult0 = mult0;
     p.multf = (float)mult;
     p.mult0f = (float)mult0;
+    // scalar pairs as aligned complex values: contiguous lines at even
+    // offsets from an aligned base
+    auto paired = [](const T *ptr, const Layout &l) {
+        return l.estride == 1 && ((uintptr_t)ptr % sizeof(C2)) == 0 && l.outer % 2 == 0 && (l.inner == 1 || l.istride % 2 == 0);
+    };
+    p.vec_in = paired(in, lin) ? 1 : 0;
+    p.vec_out = paired(out, lout) ? 1 : 0;
     if (ctx.rec) {
         // a batch step: the tile form, run by the batch kernel's CTAs
         BOp o;
@@ -2197,6 +2212,7 @@ int jt_set_option(int option, int value) {
         if (value < 0 || value > (1 << 16)) return JT_EINVAL;
         return g_opt_tile_elems.exchange(value);
     }
+    if (option == JT_OPT_REAL_FUSED_F32) return g_opt_real_fused_f32.exchange(value ? 1 : 0);
     if (option == JT_OPT_THREEPASS_MIN_LOG2) {
         if (value < 0 || value > 30) return JT_EINVAL;
         const int64_t nv = value ? (int64_t)1 << value : 0;

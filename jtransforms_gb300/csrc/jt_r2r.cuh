@@ -49,6 +49,8 @@ struct R2rParams {
     double mult, mult0;     // output (forward) or coefficient (inverse DCT) scale, index 0 apart;
                             // realInverse: the multiplier of Z
     float multf, mult0f;
+    int vec_in, vec_out;    // 1: contiguous lines whose scalar pairs (2j, 2j+1) are aligned
+                            // complex values (the register form moves them as pairs)
 };
 
 // e^{-2 pi i k/n}, 0 < k < h, from Wr (k <= n/4)
@@ -347,17 +349,8 @@ __global__ void __launch_bounds__(R2rReg<T, H, OP>::S::NT)
     }
     const bool rows_in = p.lin.estride == 1, rows_out = p.lout.estride == 1;
     auto slot = [&](int cc, int j) -> T & { return reinterpret_cast<T *>(&buf[cc * RX + pad(j >> 1)])[j & 1]; };
-
-    for (int idx = tid; idx < tot; idx += NT) {
-        int cc, i;
-        if (rows_in) {
-            cc = idx / n;
-            i = idx - cc * n;
-        } else {
-            i = idx / lines;
-            cc = idx - i * lines;
-        }
-        T x = in[line_off(p.lin, b0 + cc) + (int64_t)i * p.lin.estride];
+    // element i of line cc into its staged position
+    auto put_in = [&](int cc, int i, T x) {
         if (OP == R2R_DCT2) {
             const int j = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
             if (p.dst && (i & 1)) x = -x;
@@ -368,10 +361,99 @@ __global__ void __launch_bounds__(R2rReg<T, H, OP>::S::NT)
             const int k = p.dst ? n - 1 - i : i;
             slot(cc, k) = x * (k == 0 ? mult0 : mult);
         }
+    };
+
+    C2 v[S::E];
+    // forward real and DHT lines loaded as pairs need no reordering: the
+    // thread's own inputs t + m TL go straight to its registers (16 or more
+    // threads per line keep those loads in 128-byte runs)
+    constexpr bool DIRECT_OK = (OP == R2R_DHT || OP == R2R_RFWD) && S::TL >= 16;
+    const bool paired_in = rows_in && p.vec_in;
+    if (paired_in && S::TL < 16) {
+        // short lines: the CTA's pairs in order (idx = tid + u NT covers
+        // lines * H <= NT * E), all E loads in flight, then staged
+        C2 x[S::E];
+#pragma unroll
+        for (int u = 0; u < S::E; u++) {
+            const int idx = tid + u * NT, cc = idx / H, j = idx - cc * H;
+            if (cc < lines) x[u] = reinterpret_cast<const C2 *>(in + line_off(p.lin, b0 + cc))[j];
+        }
+#pragma unroll
+        for (int u = 0; u < S::E; u++) {
+            const int idx = tid + u * NT, cc = idx / H, j = idx - cc * H;
+            if (cc < lines) {
+                if (OP == R2R_DHT || OP == R2R_RFWD || OP == R2R_RINV) {
+                    buf[cc * RX + pad(j)] = x[u];
+                } else {
+                    put_in(cc, 2 * j, x[u].x);
+                    put_in(cc, 2 * j + 1, x[u].y);
+                }
+            }
+        }
+    } else if (paired_in) {
+        // contiguous lines: each thread loads its 16 scalar pairs t + m TL of
+        // line c at once (all in flight), coalesced across t
+        C2 x[S::E];
+        if (c < lines) {
+            const C2 *src = reinterpret_cast<const C2 *>(in + line_off(p.lin, b0 + c));
+#pragma unroll
+            for (int m = 0; m < S::E; m++) x[m] = src[t + m * S::TL];
+        }
+        if constexpr (DIRECT_OK) {
+#pragma unroll
+            for (int m = 0; m < S::E; m++) v[m] = x[m];
+        } else if (c < lines) {
+#pragma unroll
+            for (int m = 0; m < S::E; m++) {
+                const int j = t + m * S::TL;
+                if (OP == R2R_RINV) {
+                    buf[c * RX + pad(j)] = x[m];
+                } else {
+                    put_in(c, 2 * j, x[m].x);
+                    put_in(c, 2 * j + 1, x[m].y);
+                }
+            }
+        }
+    } else {
+        // four loads in flight per thread
+        for (int base = tid; base < tot; base += 4 * NT) {
+            T xs[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int idx = base + u * NT;
+                if (idx < tot) {
+                    int cc, i;
+                    if (rows_in) {
+                        cc = idx / n;
+                        i = idx - cc * n;
+                    } else {
+                        i = idx / lines;
+                        cc = idx - i * lines;
+                    }
+                    xs[u] = in[line_off(p.lin, b0 + cc) + (int64_t)i * p.lin.estride];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int idx = base + u * NT;
+                if (idx < tot) {
+                    int cc, i;
+                    if (rows_in) {
+                        cc = idx / n;
+                        i = idx - cc * n;
+                    } else {
+                        i = idx / lines;
+                        cc = idx - i * lines;
+                    }
+                    put_in(cc, i, xs[u]);
+                }
+            }
+        }
     }
     __syncthreads();
-    C2 v[S::E];
-    if (r2r_inverse(OP)) {
+    if (DIRECT_OK && paired_in) {
+        // v holds the inputs already
+    } else if (r2r_inverse(OP)) {
         // this thread's inputs Z_k, k = t + m TL, from the staged line
         const T zm = OP == R2R_RINV ? mult : (T)1;
         auto get = [&](int j) -> T { return slot(c, j); };
@@ -388,6 +470,37 @@ __global__ void __launch_bounds__(R2rReg<T, H, OP>::S::NT)
         S::run_all(v, t, buf, xi, Wp, store);
     }
     __syncthreads();
+    if ((OP == R2R_RFWD || OP == R2R_RINV) && rows_out && p.vec_out) {
+        if (OP == R2R_RINV) {
+            // the inverse FFT's h complex values are the n reals in order
+            const int totc = lines * H;
+            for (int idx = tid; idx < totc; idx += NT) {
+                const int cc = idx / H, j = idx - cc * H;
+                reinterpret_cast<C2 *>(out + line_off(p.lout, b0 + cc))[j] = buf[cc * RX + pad(j)];
+            }
+        } else {
+            // packed realForward: pair kk gives X_kk and X_{h-kk}, each one
+            // aligned (re, im) store
+            constexpr int NPAIR = H / 2 + 1;
+            const int totp = lines * NPAIR;
+            for (int idx = tid; idx < totp; idx += NT) {
+                const int cc = idx / NPAIR, kk = idx - cc * NPAIR;
+                C2 *o = reinterpret_cast<C2 *>(out + line_off(p.lout, b0 + cc));
+                const C2 *zl = buf + cc * RX;
+                if (kk == 0) {
+                    const C2 z0 = zl[0];
+                    o[0] = mk<T>(z0.x + z0.y, z0.x - z0.y);
+                    continue;
+                }
+                const C2 zk = zl[pad(kk)], zh = zl[pad(H - kk)];
+                const C2 a = mk<T>(zk.x + zh.x, zk.y - zh.y), d = mk<T>(zk.x - zh.x, zk.y + zh.y);
+                const C2 wd = cmul<T>(r2r_wr<T>(Wr, kk, H), d);
+                o[kk] = mk<T>((T)0.5 * (a.x + wd.y), (T)0.5 * (a.y - wd.x));
+                if (2 * kk != H) o[H - kk] = mk<T>((T)0.5 * (a.x - wd.y), (T)0.5 * (-a.y - wd.x));
+            }
+        }
+        return;
+    }
     r2r_store<OP, T>(buf, RX, out, p, b0, lines, Wr, Wd, mult, mult0, tid, NT);
 }
 
