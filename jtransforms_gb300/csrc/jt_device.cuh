@@ -312,6 +312,40 @@ __device__ void pass_generic(const C2 *__restrict__ src, C2 *__restrict__ dst, i
     const int total = lines * nb;
     const int step = L / (Ns * R);
     const int rstep = L / R;
+    if (total < (int)blockDim.x) {
+        // fewer butterflies than threads (a prime line is one butterfly): one
+        // thread per output k of a butterfly, each forming its own sum in
+        // the same order as below
+        const int items = total * R;
+        for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
+            const int q = idx / R, k = idx - q * R;
+            const int c = q / nb, j = q - c * nb;
+            const C2 *s = src + c * Lp;
+            const int jm = j % Ns;
+            T sr = 0, si = 0;
+            int e = 0;  // k m mod R
+            for (int m = 0; m < R; m++) {
+                C2 x = s[pad(j + m * nb)];
+                if (jm && m) {
+                    const C2 w = __ldg(&W[jm * m * step]);
+                    x = SIGN < 0 ? cmul<T>(x, w) : cmulc<T>(x, w);
+                }
+                if (m == 0) {
+                    sr = x.x;
+                    si = x.y;
+                } else {
+                    C2 w = __ldg(&W[e * rstep]);
+                    if (SIGN > 0) w.y = -w.y;
+                    sr += x.x * w.x - x.y * w.y;
+                    si += x.x * w.y + x.y * w.x;
+                }
+                e += k;
+                if (e >= R) e -= R;
+            }
+            dst[c * Lp + pad((j - jm) * R + jm + k * Ns)] = mk<T>(sr, si);
+        }
+        return;
+    }
     for (int q = threadIdx.x; q < total; q += blockDim.x) {
         int c = q / nb;
         int j = q - c * nb;
