@@ -313,7 +313,8 @@ def other_workloads(args, peak, flush, stream):
     from jtransforms_gb300 import _native as N
     out = {}
     rng = np.random.default_rng(SEED)
-    steps, warm = max(args.steps, 3), args.warmup
+    # median and best of at least 20 runs after the warm-up
+    steps, warm = max(args.steps, 20), args.warmup
     # compute rooflines: CUDA-core FMA throughput measured on this GPU
     fma = {}
     for key, prec in (("fp64", N.FLOAT64), ("fp32", N.FLOAT32)):
@@ -522,10 +523,10 @@ def mixed_batch(args, rng, flush, stream):
         b32.copy_(p32)
         b64.copy_(p64)
 
-    steps, warm = max(args.steps, 3), max(args.warmup, 2)
+    steps, warm = max(args.steps, 20), max(args.warmup, 2)
     t_graph = timed_calls([lambda: batch.run_graph()], restore, flush, steps, warm, stream)[0]
     t_pers = timed_calls([lambda: batch.run()], restore, flush, steps, warm, stream)[0]
-    t_each = timed_calls([lambda: batch.run_per_transform()], restore, flush, max(2, steps // 2), 1, stream)[0]
+    t_each = timed_calls([lambda: batch.run_per_transform()], restore, flush, 5, 1, stream)[0]
     mg, mp, me = statistics.median(t_graph), statistics.median(t_pers), statistics.median(t_each)
     # time per kind and size class: the same descriptors split into batches
     # of one kind (power of two, 7-smooth, Bluestein for the FFT kinds)
@@ -659,7 +660,7 @@ def run_ours(args, world, rank, local):
     tc = {}
     for i, n in enumerate(SIZES):
         plans[i].plan.set_mode(N.MODE_TC_SPLIT)
-        tt = timed_calls([fns[i]], lambda _, i=i: work[i].copy_(pristine[i]), flush, max(args.steps, 3), 2, stream)[0]
+        tt = timed_calls([fns[i]], lambda _, i=i: work[i].copy_(pristine[i]), flush, max(args.steps, 20), 2, stream)[0]
         ms = statistics.median(tt)
         tc[f"2^{int(math.log2(n))}"] = {
             "ms": ms, "GB/s": 2 * 8 * ELEMS / (ms * 1e-3) / 1e9, "GFLOP/s": flops_c2c(n, ELEMS // n) / (ms * 1e-3) / 1e9,
@@ -729,7 +730,9 @@ def run_ours(args, world, rank, local):
     line["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_cpu:
         v, th, desc = cpu_sample(3.0)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": desc}
+        v1, _, _ = cpu_sample(1.5, threads=1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": desc,
+                                "serial_loop": {"value": v1, "unit": UNIT, "cores": 1}}
     if rank == 0 and not args.no_other:
         del pristine
         torch.cuda.empty_cache()

@@ -28,6 +28,12 @@ ITEMS = [
     ("dst", "f32", "inv", True, [32, 210, 4096]),
     ("fft", "f64", "ci", True, [97, 1021]),
     ("dct", "f32", "fwd", True, [210, 1024, 7]),
+    # primes whose Bluestein convolution is too long for one task: separate
+    # steps over a 7-smooth convolution (12289: a two-pass 24576-point one)
+    ("fft", "f32", "cf", False, [4481, 12289]),
+    ("fft", "f32", "rf", False, [4801]),
+    ("fft", "f64", "ci", True, [2251]),
+    ("dct", "f64", "fwd", True, [2521]),
 ]
 
 
