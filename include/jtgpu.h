@@ -188,6 +188,10 @@ int jt_batch_destroy(jt_batch *batch);
 #define JT_OPT_REAL_FUSED_F32 11 /* 1 (default): Float packed realForward/realInverse lines with a
                                      power-of-two half length of 16..4096 run as one kernel (FFT and
                                      real split together); 0: the pipelined FFT and a separate split */
+#define JT_OPT_RADIX_ORDER 12   /* pass order of the mixed-radix tile kernel: -1 (default) the tuned
+                                     table of jt_plan_table.h; 0 power-of-two radices (16s) first,
+                                     1 odd radices first, 2 power-of-two radices as 8s first, 3 odd
+                                     first then 8s; plans created afterwards; the autotuner's probe */
 /* Sets a global option; returns the previous value, or JT_EINVAL. */
 int jt_set_option(int option, int value);
 

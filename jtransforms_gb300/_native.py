@@ -56,7 +56,7 @@ SIGNATURES = {
 OPT_TMA_PIPELINE, OPT_DIRECT_MAX_F32, OPT_DIRECT_MAX_F64, OPT_COLUMN_KERNEL, OPT_TWOPASS_CHUNK_MB = 0, 1, 2, 3, 4
 OPT_THREEPASS_MIN_LOG2, OPT_HOST_PIECE_MB = 5, 6
 OPT_ARENA_LIMIT_MB, OPT_BATCH_WAIT_POLLS, OPT_BATCH_STALL_TEST = 7, 8, 9
-OPT_TILE_ELEMS, OPT_REAL_FUSED_F32 = 10, 11
+OPT_TILE_ELEMS, OPT_REAL_FUSED_F32, OPT_RADIX_ORDER = 10, 11, 12
 
 _lib = None
 _lock = threading.Lock()

@@ -24,8 +24,16 @@ CTA (which sets the lines and threads per CTA), through JT_OPT_TILE_ELEMS,
 and writes the fastest into kTileElemsF32 / kTileElemsF64
 (`plan_table_tile.json`).
 
+With `--radix` it tunes the tile kernel's pass order: for each size class and
+precision it times two lengths of the class, 3 * 2^(k-2) and 7 * 2^(k-3),
+over 256 MiB batches with each of the four orders of JT_OPT_RADIX_ORDER
+(power-of-two or odd radices first; 16s or 8s for the power of two), and
+writes the order with the least summed time into kRadixOrderF32 /
+kRadixOrderF64 (`plan_table_radix_<prec>.json`).
+
     python -m jtransforms_gb300.autotune [--prec f32|f64|both] [--lo 11] [--hi 26] [--mib 1024] [--out-dir DIR]
     python -m jtransforms_gb300.autotune --tile [--prec f32|f64|both] [--out-dir DIR]
+    python -m jtransforms_gb300.autotune --radix [--prec f32|f64|both] [--out-dir DIR]
 """
 from __future__ import annotations
 
@@ -89,7 +97,7 @@ def read_header(path: str) -> dict:
     """The rows of the current tables: {prec: {lg: split}} for the pass
     splits and {"tile_" + prec: {lg: elements}} for the tile kernel."""
     import re
-    out = {"f32": {}, "f64": {}, "tile_f32": {}, "tile_f64": {}}
+    out = {"f32": {}, "f64": {}, "tile_f32": {}, "tile_f64": {}, "radix_f32": {}, "radix_f64": {}}
     if not os.path.exists(path):
         return out
     text = open(path).read()
@@ -107,6 +115,12 @@ def read_header(path: str) -> dict:
             for lg, v in enumerate(int(x) for x in m.group(1).split(",")):
                 if v > 0:
                     out["tile_" + prec][lg] = v
+    for prec, name in (("f32", "kRadixOrderF32"), ("f64", "kRadixOrderF64")):
+        m = re.search(name + r"\[14\] = \{(.*?)\};", text, re.S)
+        if m:
+            for lg, v in enumerate(int(x) for x in m.group(1).split(",")):
+                if v > 0:
+                    out["radix_" + prec][lg] = v
     return out
 
 
@@ -130,13 +144,17 @@ def write_header(best: dict, path: str):
                  "// Elements per CTA of the generic tile kernel (mixed-radix lengths), indexed\n"
                  "// by ceil(log2 L); 0: the default (4096 float, 2048 double).\n"
                  "static const short kTileElemsF32[14] = {" + tiles(best.get("tile_f32", {})) + "};\n"
-                 "static const short kTileElemsF64[14] = {" + tiles(best.get("tile_f64", {})) + "};\n")
+                 "static const short kTileElemsF64[14] = {" + tiles(best.get("tile_f64", {})) + "};\n\n"
+                 "// Pass order of the generic tile kernel (direct_radices' `order`), indexed by\n"
+                 "// ceil(log2 L); 0: power-of-two radices (16s) first.\n"
+                 "static const signed char kRadixOrderF32[14] = {" + tiles(best.get("radix_f32", {})) + "};\n"
+                 "static const signed char kRadixOrderF64[14] = {" + tiles(best.get("radix_f64", {})) + "};\n")
 
 
 def time_tile(N, J, torch, n, elems, prec, flush, steps=5, warmup=3):
     P = N.FLOAT32 if prec == "f32" else N.FLOAT64
     esz = 8 if prec == "f32" else 16
-    prev = N.set_option(N.OPT_TILE_ELEMS, elems)
+    prev = N.set_option(N.OPT_TILE_ELEMS, elems) if elems else None
     try:
         f = (J.FloatFFT_1D if prec == "f32" else J.DoubleFFT_1D)(n)
         batch = max(1, (256 << 20) // (esz * n))
@@ -156,7 +174,37 @@ def time_tile(N, J, torch, n, elems, prec, flush, steps=5, warmup=3):
         assert f.plan.algorithm(0) == 0  # one tile pass
         return {"ms": ms, "GB/s": 2 * esz * n * batch / (ms * 1e-3) / 1e9, "batch": batch}
     finally:
-        N.set_option(N.OPT_TILE_ELEMS, prev)
+        if elems:
+            N.set_option(N.OPT_TILE_ELEMS, prev)
+
+
+def time_radix(N, J, torch, n, order, prec, flush, steps=5, warmup=3):
+    prev = N.set_option(N.OPT_RADIX_ORDER, order)
+    try:
+        return time_tile(N, J, torch, n, 0, prec, flush, steps, warmup)
+    finally:
+        N.set_option(N.OPT_RADIX_ORDER, prev)
+
+
+def tune_radix(N, J, torch, precs, flush, out_dir):
+    best = {}
+    for prec in precs:
+        res, tab = {}, {}
+        for lg in range(4, 14 if prec == "f32" else 13):
+            lengths = [3 << (lg - 2), 7 << (lg - 3)]  # both with ceil(log2 n) = lg
+            cand = {}
+            for order in range(4):
+                cand[str(order)] = {str(n): time_radix(N, J, torch, n, order, prec, flush) for n in lengths}
+            total = {k: sum(v["ms"] for v in c.values()) for k, c in cand.items()}
+            key = min(total, key=total.get)
+            tab[lg] = int(key)
+            res[lg] = {"lengths": lengths, "best": int(key), "summed_ms": total, "candidates": cand}
+            print(f"radix order {prec} class 2^{lg} {lengths}: best {key} "
+                  f"({total[key]:.3f} ms against {total['0']:.3f} ms for order 0)", flush=True)
+        best["radix_" + prec] = tab
+        with open(os.path.join(out_dir, f"plan_table_radix_{prec}.json"), "w") as fh:
+            json.dump({"device": torch.cuda.get_device_name(0), "mib_per_call": 256, "sizes": res}, fh, indent=1)
+    return best
 
 
 def tune_tiles(N, J, torch, precs, flush, out_dir):
@@ -190,6 +238,7 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--out-dir", default="", help="where to write the header and the JSON (default: the package)")
     ap.add_argument("--tile", action="store_true", help="tune the mixed-radix tile kernel's elements per CTA")
+    ap.add_argument("--radix", action="store_true", help="tune the mixed-radix tile kernel's pass order")
     args = ap.parse_args(argv)
     import torch
     sys.path.insert(0, os.path.dirname(HERE))
@@ -210,6 +259,10 @@ def main(argv=None) -> int:
     precs = ["f32", "f64"] if args.prec == "both" else [args.prec]
     if args.tile:
         best.update(tune_tiles(N, J, torch, precs, flush, args.out_dir or HERE))
+        write_header(best, header)
+        return 0
+    if args.radix:
+        best.update(tune_radix(N, J, torch, precs, flush, args.out_dir or HERE))
         write_header(best, header)
         return 0
     for prec in precs:

@@ -281,22 +281,48 @@ template <typename T> struct Lim {
 };
 
 // Radices for a DIRECT line; empty if n has a prime factor > 63.
-static std::vector<int> direct_radices(int64_t n) {
-    std::vector<int> r;
+// Pass radices of the tile kernel for n, in the pass order `order`: bit 0
+// puts the odd factors (7, 5, 3, then the other odd ones up to 63) before the
+// power-of-two part instead of after it; bit 1 splits the power of two into
+// 8s (then 4 or 2) instead of 16s (then 8, 4 or 2).  Empty if n has a prime
+// factor > 63.  Every order computes the same DFT; the tuned order per size
+// class comes from radix_order.
+static std::vector<int> direct_radices(int64_t n, int order = 0) {
+    std::vector<int> p2, odd;
     int64_t m = n;
     int a = 0;
     while (m % 2 == 0) { m /= 2; a++; }
-    while (a >= 4) { r.push_back(16); a -= 4; }
-    if (a == 3) r.push_back(8);
-    else if (a == 2) r.push_back(4);
-    else if (a == 1) r.push_back(2);
+    if (order & 2) {
+        while (a >= 3) { p2.push_back(8); a -= 3; }
+        if (a == 2) p2.push_back(4);
+        else if (a == 1) p2.push_back(2);
+    } else {
+        while (a >= 4) { p2.push_back(16); a -= 4; }
+        if (a == 3) p2.push_back(8);
+        else if (a == 2) p2.push_back(4);
+        else if (a == 1) p2.push_back(2);
+    }
     for (int p : {7, 5, 3})
-        while (m % p == 0) { r.push_back(p); m /= p; }
+        while (m % p == 0) { odd.push_back(p); m /= p; }
     for (int p = 11; p <= 63 && m > 1; p += 2)
-        while (m % p == 0) { r.push_back(p); m /= p; }
-    if (m != 1) r.clear();
-    if (n == 1) r.clear();
+        while (m % p == 0) { odd.push_back(p); m /= p; }
+    if (m != 1 || n == 1) return {};
+    std::vector<int> r = (order & 1) ? odd : p2;
+    const std::vector<int> &tail = (order & 1) ? p2 : odd;
+    r.insert(r.end(), tail.begin(), tail.end());
     return r;
+}
+
+// Tuned pass order (direct_radices) for the tile kernel's length n: the
+// probe option, else the table by ceil(log2 n) (jt_plan_table.h).
+static std::atomic<int> g_opt_radix_order{-1};
+static int radix_order(int64_t n, bool f32) {
+    const int o = g_opt_radix_order.load();
+    if (o >= 0) return o;
+    int lg = 0;
+    while (((int64_t)1 << lg) < n) lg++;
+    if (lg >= 14) return 0;
+    return f32 ? kRadixOrderF32[lg] : kRadixOrderF64[lg];
 }
 
 template <typename T> struct Fft1 {
@@ -405,7 +431,7 @@ template <typename T> struct Fft1 {
     int init_direct() {
         algo = ALG_DIRECT;
         JT_TRY(set_reg(reg_ok(n)));
-        if (!reg) radix = direct_radices(n);
+        if (!reg) radix = direct_radices(n, radix_order(n, sizeof(T) == 4));
         return make_roots(&W, n, 1, n);
     }
 
@@ -421,7 +447,7 @@ template <typename T> struct Fft1 {
         for (Fft1 *sub : {pa.get(), pb.get()})
             if (sub->reg && sub->n > 4096) {
                 sub->reg = false;
-                sub->radix = direct_radices(sub->n);
+                sub->radix = direct_radices(sub->n, radix_order(sub->n, sizeof(T) == 4));
             }
         return make_twiddle_pair(n, &Whi, &Wlo, &lo_bits);
     }
@@ -555,7 +581,7 @@ template <typename T> struct Fft1 {
         memset(&p, 0, sizeof(p));
         p.n = (int)n;
         p.nB = (int)nB;
-        std::vector<int> rr = direct_radices(nB);
+        std::vector<int> rr = direct_radices(nB, radix_order(nB, sizeof(T) == 4));
         if (rr.empty() || (int)rr.size() > JT_MAX_PASSES) return JT_EINVAL;
         p.npass = (int)rr.size();
         for (int i = 0; i < p.npass; i++) p.radix[i] = rr[i];
@@ -623,7 +649,7 @@ template <typename T> struct Fft1 {
             int cmax = (int)std::max<size_t>(1, std::min<size_t>(g_smem_optin, JT_BATCH_SMEM_CAP) / per_line);
             C = std::min(C, cmax);
             if ((int64_t)C > nlines) C = (int)nlines;
-            std::vector<int> rr = radix.empty() ? direct_radices(n) : radix;
+            std::vector<int> rr = radix.empty() ? direct_radices(n, radix_order(n, sizeof(T) == 4)) : radix;
             o.type = BOP_TILE;
             o.tp.L = L;
             o.tp.npass = (int)rr.size();
@@ -1147,7 +1173,7 @@ static int r2r_fused(Ctx &ctx, int op, const Real1<T> *rf, const T *in, T *out, 
     typedef typename V2<T>::t C2;
     if (nlines <= 0) return JT_OK;
     const int64_t n = rf->n, h = n / 2;
-    std::vector<int> rr = direct_radices(h);
+    std::vector<int> rr = direct_radices(h, radix_order(h, sizeof(T) == 4));
     if (rr.empty() || (int)rr.size() > JT_MAX_PASSES) return JT_EINVAL;
     R2rParams p;
     memset(&p, 0, sizeof(p));
@@ -2213,6 +2239,12 @@ int jt_set_option(int option, int value) {
         return g_opt_tile_elems.exchange(value);
     }
     if (option == JT_OPT_REAL_FUSED_F32) return g_opt_real_fused_f32.exchange(value ? 1 : 0);
+    if (option == JT_OPT_RADIX_ORDER) {
+        if (value < -1 || value > 3) return JT_EINVAL;
+        const int prev = g_opt_radix_order.exchange(value);
+        if (prev != value) g_plan_gen++;  // plans fix their radices at creation
+        return prev;
+    }
     if (option == JT_OPT_THREEPASS_MIN_LOG2) {
         if (value < 0 || value > 30) return JT_EINVAL;
         const int64_t nv = value ? (int64_t)1 << value : 0;

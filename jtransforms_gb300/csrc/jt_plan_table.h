@@ -23,3 +23,8 @@ static const signed char kSplitF64[31][3] = {
 // by ceil(log2 L); 0: the default (4096 float, 2048 double).
 static const short kTileElemsF32[14] = {0, 0, 0, 0, 512, 512, 512, 1024, 1024, 1024, 1024, 2048, 4096, 8192};
 static const short kTileElemsF64[14] = {0, 0, 0, 0, 512, 512, 512, 512, 1024, 2048, 2048, 2048, 4096, 0};
+
+// Pass order of the generic tile kernel (direct_radices' `order`), indexed by
+// ceil(log2 L); 0: power-of-two radices (16s) first.
+static const signed char kRadixOrderF32[14] = {0, 0, 0, 0, 1, 3, 0, 0, 2, 0, 0, 0, 0, 0};
+static const signed char kRadixOrderF64[14] = {0, 0, 0, 0, 1, 1, 0, 0, 2, 0, 0, 2, 0, 0};
