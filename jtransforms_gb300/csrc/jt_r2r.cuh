@@ -2,9 +2,13 @@
 // kernel each: one HBM round trip per axis, on contiguous or strided lines.
 //
 // A CTA holds C lines of n reals as C complex lines of h = n/2 in shared
-// memory and runs the h-point complex FFT on them with the tile passes
-// (jt_device.cuh).  Around it (Makhoul's reordering, the standard real-FFT
-// split and the DCT quarter-wave twiddle):
+// memory and runs the h-point complex FFT on them: in registers with the
+// Stockham core for power-of-two h from 16 to 4096 (r2r_reg_kernel), else
+// with the tile passes of jt_device.cuh (r2r_tile_kernel, also the batch's
+// one-step form).  Contiguous lines whose scalar pairs are aligned complex
+// values move as pairs, the rest one scalar at a time.  Around the FFT
+// (Makhoul's reordering, the standard real-FFT split and the DCT
+// quarter-wave twiddle):
 //   forward DCT/DST   load:  v_j = x_2j, v_{n-1-j} = x_2j+1 (DST: odd
 //                            inputs negated), z_m = v_2m + i v_2m+1
 //                     store: V_k from Z_k and Z_{h-k}, C_k = Re(e^{-i pi k/2n}
@@ -20,7 +24,8 @@
 //   realInverse       load:  the packed spectrum; Z_k from X_k and X_{h-k};
 //                     store: x_2m + i x_2m+1 = z_m after the e^{+} FFT
 // The arithmetic is the same as the separate pre/post kernels of
-// jt_device.cuh, which the batch recorder and odd lengths still use.
+// jt_device.cuh, which odd lengths and half lengths the tile passes do not
+// take still use.
 // Reference: dct/DoubleDCT_1D.java:169-440, dst/DoubleDST_1D.java:96-328,
 // dht/DoubleDHT_1D.java:94-276, fft/DoubleFFT_1D.java:524-561 (realForward,
 // rftfsub) and :946-989 (realInverse, rftbsub).
