@@ -423,36 +423,24 @@ __global__ void __launch_bounds__(R2rReg<T, H, OP>::S::NT)
         // four loads in flight per thread
         for (int base = tid; base < tot; base += 4 * NT) {
             T xs[4];
+            int cs[4], is[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const int idx = base + u * NT;
                 if (idx < tot) {
-                    int cc, i;
                     if (rows_in) {
-                        cc = idx / n;
-                        i = idx - cc * n;
+                        cs[u] = idx / n;
+                        is[u] = idx - cs[u] * n;
                     } else {
-                        i = idx / lines;
-                        cc = idx - i * lines;
+                        is[u] = idx / lines;
+                        cs[u] = idx - is[u] * lines;
                     }
-                    xs[u] = in[line_off(p.lin, b0 + cc) + (int64_t)i * p.lin.estride];
+                    xs[u] = in[line_off(p.lin, b0 + cs[u]) + (int64_t)is[u] * p.lin.estride];
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int idx = base + u * NT;
-                if (idx < tot) {
-                    int cc, i;
-                    if (rows_in) {
-                        cc = idx / n;
-                        i = idx - cc * n;
-                    } else {
-                        i = idx / lines;
-                        cc = idx - i * lines;
-                    }
-                    put_in(cc, i, xs[u]);
-                }
-            }
+            for (int u = 0; u < 4; u++)
+                if (base + u * NT < tot) put_in(cs[u], is[u], xs[u]);
         }
     }
     __syncthreads();
