@@ -784,6 +784,12 @@ def profile_case(case: str) -> int:
         plan = J.DoubleDST_3D(128, 128, 128).plan
         x = torch.from_numpy(rng.uniform(-1, 1, 128 ** 3)).cuda()
         run = lambda: plan.execute(N.FORWARD, x, 0, True)  # noqa: E731
+    elif case == "tile1000":  # DoubleFFT_1D(1000) on 256 MiB: the mixed-radix tile kernel, one pass
+        n = 1000
+        B = (256 << 20) // (16 * n)
+        plan = J.DoubleFFT_1D(n).plan
+        x = torch.from_numpy(rng.uniform(-1, 1, 2 * n * B)).cuda()
+        run = lambda: plan.execute(N.COMPLEX_FORWARD, x, 0, False, batch=B, dist=2 * n)  # noqa: E731
     elif case == "batch":  # the 10,000 mixed transforms, one persistent launch per call
         items_batch = mixed_batch_items(rng)
         bt = N.Batch(items_batch[0])
@@ -822,7 +828,7 @@ def main():
     ap.add_argument("--chunk-mb", type=int, default=0, help="MiB of transforms per two-pass chunk (library default 1024)")
     ap.add_argument("--host-piece-mb", type=int, default=0, help="MiB per piece of the end-to-end host batch (library default 64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
-    ap.add_argument("--case", default="", choices=["", "c1", "c2a", "c2b", "c3b", "tc1024", "batch", "peaks"],
+    ap.add_argument("--case", default="", choices=["", "c1", "c2a", "c2b", "c3b", "tc1024", "tile1000", "batch", "peaks"],
                     help="profiling case: run one small workload a few times and exit (no JSON line)")
     args = ap.parse_args()
     global ELEMS, SIZES
